@@ -1,0 +1,492 @@
+// cf_engine.cu -- host side of the C-ABI (include/contrafold_gb300.h).
+//
+// An engine owns the device parameter blobs, a stream and a growable work
+// arena.  Every batch call: validate -> plan (order sequences, assign groups
+// and arena slices within the memory budget) -> upload inputs once -> launch
+// the phase kernels per slice -> download outputs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/contrafold_gb300.h"
+#include "cf_kernels.h"
+#include "cf_sample.h"
+
+
+using cf::SeqDesc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CF_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? CF_ENOMEM : CF_ECUDA,            \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));               \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;   // elements
+    int ensure(size_t n) {
+        if (n <= cap) return CF_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, 1);
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(CF_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        cap = want;
+        return CF_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+enum Job { JOB_LOGZ = 0, JOB_LOGZ64, JOB_BPP, JOB_MEA, JOB_MFE, JOB_SAMPLE };
+
+int64_t arena_words(Job job, int L) {
+    switch (job) {
+        case JOB_LOGZ:
+        case JOB_SAMPLE: return cf::pad32(cf::arena32_inside_words(L));
+        case JOB_LOGZ64:
+        case JOB_MFE: return cf::arena64(L).total;
+        default: return cf::arena32(L).total;
+    }
+}
+
+}  // namespace
+
+struct cf_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf<float> blob32;
+    DevBuf<double> blob64;
+    DevBuf<float> arena;
+    DevBuf<uint8_t> seqs, mask;
+    DevBuf<SeqDesc> descs;
+    DevBuf<float> logz;
+    DevBuf<double> logz64;
+    DevBuf<char> structs;
+    DevBuf<float> post;
+    DevBuf<int64_t> post_offs;
+    DevBuf<int> status;
+    DevBuf<char> samples;
+    size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
+    int mode = 1;        // 0 plain, 1 batched
+    size_t smem_optin = 0;
+};
+
+namespace {
+
+// ---- group-size autotune table: sequences per CTA by length range ----
+// Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
+int group_for_length(int L) {
+    if (L <= 64) return 8;
+    if (L <= 160) return 4;
+    if (L <= 320) return 2;
+    return 1;
+}
+
+struct Plan {
+    std::vector<SeqDesc> descs;   // grouped order
+    std::vector<int> slice_begin; // descs index where each arena slice starts (group aligned)
+    std::vector<int64_t> slice_words;
+    int group = 1;
+    int Lmax = 0;
+};
+
+int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
+    P.descs.resize(n);
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    P.group = 1;
+    P.Lmax = 0;
+    for (int b = 0; b < n; ++b) P.Lmax = std::max<int>(P.Lmax, (int)(offsets[b + 1] - offsets[b]));
+    const bool batched = eng->mode == 1;
+    if (batched) {
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
+        });
+        // one group size for the launch: that of the median length
+        const int Lmed = n ? (int)(offsets[order[n / 2] + 1] - offsets[order[n / 2]]) : 0;
+        P.group = std::min(cf::kMaxGroup, group_for_length(Lmed));
+    }
+    for (int k = 0; k < n; ++k) {
+        const int b = order[k];
+        P.descs[k].seq_off = offsets[b];
+        P.descs[k].L = (int)(offsets[b + 1] - offsets[b]);
+        P.descs[k].idx = b;
+    }
+    // arena slices within the budget
+    size_t budget = eng->budget;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        budget = fr / 2;
+    }
+    const int64_t budget_words = (int64_t)(budget / 4);
+    P.slice_begin.clear();
+    P.slice_words.clear();
+    int64_t cur = 0;
+    int start = 0;
+    for (int k = 0; k < n; k += P.group) {
+        int64_t gw = 0;
+        const int kend = std::min(n, k + P.group);
+        for (int t = k; t < kend; ++t) gw += arena_words(job, P.descs[t].L);
+        if (gw > budget_words) return fail(CF_ENOMEM, "sequence group does not fit the arena budget");
+        if (cur + gw > budget_words && k > start) {
+            P.slice_begin.push_back(start);
+            P.slice_words.push_back(cur);
+            start = k;
+            cur = 0;
+        }
+        for (int t = k; t < kend; ++t) {
+            P.descs[t].ws_off = cur;
+            cur += arena_words(job, P.descs[t].L);
+        }
+    }
+    P.slice_begin.push_back(start);
+    P.slice_words.push_back(cur);
+    P.slice_begin.push_back(n);
+    return CF_OK;
+}
+
+int check_batch(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets, int32_t n) {
+    if (!eng) return fail(CF_EINVAL, "engine is NULL");
+    if (n < 0) return fail(CF_EINVAL, "negative batch size");
+    if (n > 0 && !offsets) return fail(CF_EINVAL, "offsets is NULL");
+    if (n > 0 && offsets[0] != 0) return fail(CF_EINVAL, "offsets[0] must be 0");
+    for (int b = 0; b < n; ++b) {
+        const int64_t L = offsets[b + 1] - offsets[b];
+        if (L < 0) return fail(CF_EINVAL, "offsets must be non-decreasing");
+        if (L > CF_MAX_LEN) return fail(CF_EINVAL, "sequence longer than CF_MAX_LEN");
+    }
+    if (n > 0 && offsets[n] > 0 && !seqs) return fail(CF_EINVAL, "seqs is NULL");
+    return CF_OK;
+}
+
+int ensure_smem(cf_engine* eng, size_t bytes) {
+    if (bytes <= 48 * 1024) return CF_OK;
+    if (bytes <= eng->smem_optin) return CF_OK;
+    int dev_max = 0;
+    CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device));
+    if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");
+    const void* ks[] = {(const void*)cf::k_inside32, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
+                        (const void*)cf::k_posterior32, (const void*)cf::k_mea32, (const void*)cf::k_viterbi64};
+    for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    eng->smem_optin = bytes;
+    return CF_OK;
+}
+
+// Runs `job` over a batch whose inputs are already on the device.
+struct SampleJob {
+    int n_samples = 0;
+    uint64_t seed = 0;
+    char* d_out = nullptr;
+};
+
+int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, const uint8_t* d_mask, float gamma,
+               float* d_logz, double* d_logz64, char* d_structs, float* d_post, const int64_t* d_post_offs,
+               cudaStream_t st, const SampleJob* sj = nullptr) {
+    const int n = (int)P.descs.size();
+    if (n == 0) return CF_OK;
+    int rc = eng->descs.ensure(n);
+    if (rc) return rc;
+    CF_CUDA(cudaMemcpyAsync(eng->descs.p, P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice, st));
+    int64_t maxw = 0;
+    for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
+    if ((rc = eng->arena.ensure((size_t)std::max<int64_t>(maxw, 1)))) return rc;
+    if ((rc = eng->status.ensure(1))) return rc;
+    CF_CUDA(cudaMemsetAsync(eng->status.p, 0, sizeof(int), st));
+    const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
+    const size_t smem = cf::fold_smem_bytes(P.Lmax, P.group, fp64);
+    if ((rc = ensure_smem(eng, smem))) return rc;
+
+    for (size_t s = 0; s + 1 < P.slice_begin.size(); ++s) {
+        const int k0 = P.slice_begin[s], k1 = P.slice_begin[s + 1];
+        cf::FoldArgs A;
+        A.descs = eng->descs.p + k0;
+        A.n = k1 - k0;
+        A.group = P.group;
+        A.seqs = d_seqs;
+        A.mask = d_mask;
+        A.blob32 = eng->blob32.p;
+        A.blob64 = eng->blob64.p;
+        A.ws = eng->arena.p;
+        A.logz = d_logz;
+        A.logz64 = d_logz64;
+        A.structs = d_structs;
+        A.post_out = d_post;
+        A.post_offs = d_post_offs;
+        A.gamma = gamma;
+        A.status = eng->status.p;
+        const int grid = (A.n + P.group - 1) / P.group;
+        const dim3 blk(cf::kFoldThreads);
+        switch (job) {
+            case JOB_LOGZ:
+                cf::k_inside32<<<grid, blk, smem, st>>>(A);
+                break;
+            case JOB_LOGZ64:
+                cf::k_inside64<<<grid, blk, smem, st>>>(A);
+                break;
+            case JOB_BPP:
+            case JOB_MEA: {
+                cf::FoldArgs Ai = A;
+                Ai.logz = nullptr;
+                cf::k_inside32<<<grid, blk, smem, st>>>(Ai);
+                cf::k_outside32<<<grid, blk, smem, st>>>(A);
+                if (job == JOB_BPP) {
+                    cf::k_posterior32<<<grid, blk, smem, st>>>(A);
+                } else {
+                    cf::FoldArgs Ap = A;
+                    Ap.post_out = nullptr;
+                    Ap.logz = nullptr;
+                    cf::k_posterior32<<<grid, blk, smem, st>>>(Ap);
+                    cf::k_mea32<<<grid, blk, smem, st>>>(A);
+                }
+                break;
+            }
+            case JOB_MFE:
+                cf::k_viterbi64<<<grid, blk, smem, st>>>(A);
+                break;
+            case JOB_SAMPLE: {
+                cf::k_inside32<<<grid, blk, smem, st>>>(A);
+                CF_CUDA(cudaGetLastError());
+                if (!sj || sj->n_samples <= 0) break;
+                cf::SampleArgs S;
+                S.descs = A.descs;
+                S.n = A.n;
+                S.n_samples = sj->n_samples;
+                S.Lmax = P.Lmax;
+                S.seed = sj->seed;
+                S.seqs = d_seqs;
+                S.mask = d_mask;
+                S.blob32 = eng->blob32.p;
+                S.ws = eng->arena.p;
+                S.out = sj->d_out;
+                S.status = eng->status.p;
+                const size_t ssm = cf::sample_smem_bytes(P.Lmax);
+                if (ssm > 48 * 1024)
+                    CF_CUDA(cudaFuncSetAttribute((const void*)cf::k_sample32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)ssm));
+                const int64_t items = (int64_t)A.n * sj->n_samples;
+                const int warps = cf::sample_threads() / 32;
+                int sgrid = (int)std::min<int64_t>((items + warps - 1) / warps, 152 * 16);
+                cf::k_sample32<<<sgrid, cf::sample_threads(), ssm, st>>>(S);
+                break;
+            }
+            default:
+                return fail(CF_EINVAL, "bad job");
+        }
+        CF_CUDA(cudaGetLastError());
+    }
+    return CF_OK;
+}
+
+int read_status(cf_engine* eng, cudaStream_t st) {
+    int h = 0;
+    CF_CUDA(cudaMemcpyAsync(&h, eng->status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CF_CUDA(cudaStreamSynchronize(st));
+    if (h != CF_OK) return fail(h, "a kernel reported an internal limit (traceback stack/queue)");
+    return CF_OK;
+}
+
+// Host-buffer front end shared by the synchronous entry points.
+int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask,
+             int32_t n, float gamma, float* logz_out, double* logz64_out, char* struct_out,
+             const int64_t* post_offsets, float* post_out, int n_samples = 0, uint64_t seed = 0,
+             char* sample_out = nullptr) {
+    int rc = check_batch(eng, seqs, offsets, n);
+    if (rc) return rc;
+    if (n == 0) return CF_OK;
+    CF_CUDA(cudaSetDevice(eng->device));
+    cudaStream_t st = eng->stream;
+    Plan P;
+    if ((rc = make_plan(eng, job, offsets, n, P))) return rc;
+    const size_t nbytes = (size_t)offsets[n];
+    if ((rc = eng->seqs.ensure(nbytes))) return rc;
+    if (nbytes) CF_CUDA(cudaMemcpyAsync(eng->seqs.p, seqs, nbytes, cudaMemcpyHostToDevice, st));
+    const uint8_t* d_mask = nullptr;
+    if (mask) {
+        if ((rc = eng->mask.ensure(nbytes))) return rc;
+        if (nbytes) CF_CUDA(cudaMemcpyAsync(eng->mask.p, mask, nbytes, cudaMemcpyHostToDevice, st));
+        d_mask = eng->mask.p;
+    }
+    float* d_logz = nullptr;
+    double* d_logz64 = nullptr;
+    char* d_structs = nullptr;
+    float* d_post = nullptr;
+    int64_t* d_post_offs = nullptr;
+    size_t post_total = 0;
+    if (logz_out) {
+        if ((rc = eng->logz.ensure(n))) return rc;
+        d_logz = eng->logz.p;
+    }
+    if (logz64_out) {
+        if ((rc = eng->logz64.ensure(n))) return rc;
+        d_logz64 = eng->logz64.p;
+    }
+    if (struct_out) {
+        if ((rc = eng->structs.ensure(nbytes))) return rc;
+        d_structs = eng->structs.p;
+    }
+    if (post_out) {
+        std::vector<int64_t> po(post_offsets, post_offsets + n);
+        for (int b = 0; b < n; ++b) {
+            const int64_t L = offsets[b + 1] - offsets[b];
+            post_total = std::max<size_t>(post_total, (size_t)(po[b] + L * L));
+        }
+        if ((rc = eng->post.ensure(post_total))) return rc;
+        if ((rc = eng->post_offs.ensure(n))) return rc;
+        CF_CUDA(cudaMemcpyAsync(eng->post_offs.p, po.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st));
+        d_post = eng->post.p;
+        d_post_offs = eng->post_offs.p;
+    }
+    SampleJob sj;
+    const size_t sample_bytes = nbytes * (size_t)std::max(n_samples, 0);
+    if (job == JOB_SAMPLE && sample_bytes) {
+        if ((rc = eng->samples.ensure(sample_bytes))) return rc;
+        sj.n_samples = n_samples;
+        sj.seed = seed;
+        sj.d_out = eng->samples.p;
+    }
+    if ((rc = run_device(eng, job, P, eng->seqs.p, d_mask, gamma, d_logz, d_logz64, d_structs, d_post, d_post_offs, st,
+                         &sj)))
+        return rc;
+    if (sample_out && sample_bytes)
+        CF_CUDA(cudaMemcpyAsync(sample_out, sj.d_out, sample_bytes, cudaMemcpyDeviceToHost, st));
+    if (logz_out) CF_CUDA(cudaMemcpyAsync(logz_out, d_logz, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+    if (logz64_out) CF_CUDA(cudaMemcpyAsync(logz64_out, d_logz64, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (struct_out && nbytes) CF_CUDA(cudaMemcpyAsync(struct_out, d_structs, nbytes, cudaMemcpyDeviceToHost, st));
+    if (post_out && post_total) CF_CUDA(cudaMemcpyAsync(post_out, d_post, sizeof(float) * post_total, cudaMemcpyDeviceToHost, st));
+    return read_status(eng, st);
+}
+
+}  // namespace
+
+// ============================ C-ABI ============================
+extern "C" {
+
+const char* cf_last_error(void) { return g_err.c_str(); }
+const char* cf_version(void) { return "contrafold-gb300 0.1.0 (sm_103a)"; }
+
+int cf_engine_create(const float* params32, const double* params64, int device, cf_engine** out) {
+    if (!out || !params32 || !params64) return fail(CF_EINVAL, "NULL argument to cf_engine_create");
+    *out = nullptr;
+    int ndev = 0;
+    CF_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(CF_EINVAL, "no such CUDA device");
+    CF_CUDA(cudaSetDevice(device));
+    cf_engine* e = new cf_engine();
+    e->device = device;
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete e;
+        return fail(CF_ECUDA, "cudaStreamCreate failed");
+    }
+    int rc = cf_engine_set_params(e, params32, params64);
+    if (rc) {
+        cf_engine_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return CF_OK;
+}
+
+int cf_engine_destroy(cf_engine* e) {
+    if (!e) return CF_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->blob32.release(); e->blob64.release(); e->arena.release(); e->seqs.release(); e->mask.release();
+    e->descs.release(); e->logz.release(); e->logz64.release(); e->structs.release(); e->post.release();
+    e->post_offs.release(); e->status.release(); e->samples.release();
+
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return CF_OK;
+}
+
+int cf_engine_set_params(cf_engine* e, const float* params32, const double* params64) {
+    if (!e || !params32 || !params64) return fail(CF_EINVAL, "NULL argument to cf_engine_set_params");
+    CF_CUDA(cudaSetDevice(e->device));
+    int rc;
+    if ((rc = e->blob32.ensure(CF_BLOB_LEN))) return rc;
+    if ((rc = e->blob64.ensure(CF_BLOB_LEN))) return rc;
+    CF_CUDA(cudaMemcpyAsync(e->blob32.p, params32, sizeof(float) * CF_BLOB_LEN, cudaMemcpyHostToDevice, e->stream));
+    CF_CUDA(cudaMemcpyAsync(e->blob64.p, params64, sizeof(double) * CF_BLOB_LEN, cudaMemcpyHostToDevice, e->stream));
+    CF_CUDA(cudaStreamSynchronize(e->stream));
+    return CF_OK;
+}
+
+int cf_engine_set_budget(cf_engine* e, size_t bytes) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    e->budget = bytes;
+    return CF_OK;
+}
+
+int cf_engine_set_mode(cf_engine* e, int mode) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    if (mode != 0 && mode != 1) return fail(CF_EINVAL, "mode must be 0 (plain) or 1 (batched)");
+    e->mode = mode;
+    return CF_OK;
+}
+
+int cf_logz(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+            float* logz_out) {
+    if (n > 0 && !logz_out) return fail(CF_EINVAL, "logz_out is NULL");
+    return run_host(e, JOB_LOGZ, seqs, offsets, mask, n, 0.f, logz_out, nullptr, nullptr, nullptr, nullptr);
+}
+
+int cf_logz64(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+              double* logz_out) {
+    if (n > 0 && !logz_out) return fail(CF_EINVAL, "logz_out is NULL");
+    return run_host(e, JOB_LOGZ64, seqs, offsets, mask, n, 0.f, nullptr, logz_out, nullptr, nullptr, nullptr);
+}
+
+int cf_bpp(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+           const int64_t* post_offsets, float* post_out, float* logz_out) {
+    if (n > 0 && (!post_out || !post_offsets)) return fail(CF_EINVAL, "post_out / post_offsets is NULL");
+    return run_host(e, JOB_BPP, seqs, offsets, mask, n, 0.f, logz_out, nullptr, nullptr, post_offsets, post_out);
+}
+
+int cf_mea(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n, float gamma,
+           char* struct_out) {
+    if (n > 0 && !struct_out) return fail(CF_EINVAL, "struct_out is NULL");
+    if (!(gamma > 0.0f)) return fail(CF_EINVAL, "gamma must be > 0");
+    return run_host(e, JOB_MEA, seqs, offsets, mask, n, gamma, nullptr, nullptr, struct_out, nullptr, nullptr);
+}
+
+int cf_mfe(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+           char* struct_out) {
+    if (n > 0 && !struct_out) return fail(CF_EINVAL, "struct_out is NULL");
+    return run_host(e, JOB_MFE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, struct_out, nullptr, nullptr);
+}
+
+int cf_sample(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+              int32_t n_samples, uint64_t seed, char* out) {
+    if (n_samples < 0) return fail(CF_EINVAL, "n_samples must be >= 0");
+    if (n > 0 && n_samples > 0 && !out) return fail(CF_EINVAL, "out is NULL");
+    return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, n_samples,
+                    seed, out);
+}
+
+}  // extern "C"

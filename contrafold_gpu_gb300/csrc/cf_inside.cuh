@@ -1,0 +1,235 @@
+// cf_inside.cuh -- the inside recurrence (FC / FM1 / FM / F5) over one of
+// three semirings, evaluated one DP cell per thread on a diagonal wavefront.
+//
+//   Lse32  float32, CONTRAfold Fast_LogPlusEquals   (cpu.py:595-678, gpu.py:79-183)
+//   Lse64  float64, exact log1p/exp                 (cpu.py:165-275)
+//   Max64  float64, max-plus (Viterbi forward)      (cpu.py:302-394)
+//
+// Every cell accumulates its candidates in the reference's order -- FM2 over
+// k ascending; FC: hairpin, single-branch loops p ascending / q descending,
+// multibranch; FM1: pair, then extension; FM: FM2, extension, FM1 -- with the
+// same left-to-right additions, so the FP32 tables are bitwise equal to the
+// reference's float32 tables.
+#pragma once
+
+#include "cf_device.cuh"
+
+namespace cf {
+
+struct Lse32 {
+    using Real = float;
+    const PolyTables* pt;
+    static __device__ __forceinline__ Real neg() { return CF_NEG32; }
+    static __device__ __forceinline__ Real half() { return CF_HALF32; }
+    static __device__ __forceinline__ Real add(Real a, Real b) { return __fadd_rn(a, b); }
+    __device__ __forceinline__ Real plus(Real acc, Real x) const { return lse32(pt, acc, x); }
+};
+
+struct Lse64 {
+    using Real = double;
+    static __device__ __forceinline__ Real neg() { return CF_NEG64; }
+    static __device__ __forceinline__ Real half() { return CF_HALF64; }
+    static __device__ __forceinline__ Real add(Real a, Real b) { return __dadd_rn(a, b); }
+    __device__ __forceinline__ Real plus(Real acc, Real x) const { return lse64(acc, x); }
+};
+
+struct Max64 {
+    using Real = double;
+    static __device__ __forceinline__ Real neg() { return CF_NEG64; }
+    static __device__ __forceinline__ Real half() { return CF_HALF64; }
+    static __device__ __forceinline__ Real add(Real a, Real b) { return __dadd_rn(a, b); }
+    // strict '>' keeps the earlier value on ties, as `if v > best` does
+    __device__ __forceinline__ Real plus(Real acc, Real x) const { return x > acc ? x : acc; }
+};
+
+// Shared-memory scoring tables for semiring real type R.
+template <typename R>
+struct SmemTabs {
+    R blob[CF_BLOB_LEN + 3];
+    R jB[625];   // hc[a][b] + tm[a][b][c][d]: the reference's ScoreJunctionB sum
+};
+
+template <typename R>
+__device__ __forceinline__ void load_tabs(SmemTabs<R>* t, const R* __restrict__ g) {
+    for (int k = threadIdx.x; k < CF_BLOB_LEN; k += blockDim.x) t->blob[k] = g[k];
+    for (int k = threadIdx.x; k < 625; k += blockDim.x) {
+        const int a = k / 125, c = (k / 25) % 5;
+        const R hc = g[CF_OFF_HC + a * 5 + c];
+        const R tm = g[CF_OFF_TM + k];
+        t->jB[k] = hc + tm;   // single rounded add (fp contraction cannot apply)
+    }
+}
+
+// Inside tables of one sequence, triangular diagonal-major (see cf_device.cuh).
+template <typename R>
+struct InTabs {
+    R* FC;
+    R* FM;
+    R* FM1;
+    R* F5;
+    int m;   // L + 1
+    __device__ __forceinline__ int at(int i, int j) const { return tri_off(j - i, m) + i; }
+};
+
+// ScoreJunctionA(i, j) for the pair (i, j+1) (cpu.py:224-228).
+template <class S>
+__device__ __forceinline__ typename S::Real junctionA(const ParamView<typename S::Real>& P, int L,
+                                                      const SeqView& Q, int i, int j) {
+    using R = typename S::Real;
+    R jA = P.hc(Q.s[i], Q.s[j + 1]);
+    if (i < L) jA = S::add(jA, P.dl(Q.s[i], Q.s[j + 1], Q.s[i + 1]));
+    if (j > 0) jA = S::add(jA, P.dr(Q.s[i], Q.s[j + 1], Q.s[j]));
+    return jA;
+}
+
+// ScoreJunctionA(j, i) for the pair (i+1, j) as used by FM1 / F5 (cpu.py:237-241, 268-272).
+template <class S>
+__device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typename S::Real>& P, int L,
+                                                          const SeqView& Q, int i, int j) {
+    using R = typename S::Real;
+    R jA = P.hc(Q.s[j], Q.s[i + 1]);
+    if (j < L) jA = S::add(jA, P.dl(Q.s[j], Q.s[i + 1], Q.s[j + 1]));
+    if (i > 0) jA = S::add(jA, P.dr(Q.s[j], Q.s[i + 1], Q.s[i]));
+    return jA;
+}
+
+// One inside cell (i, j).  Writes FC, FM1, FM at (i, j) (the semiring zero
+// where the reference leaves the cell at NEG).
+template <class S>
+__device__ __forceinline__ void inside_cell(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
+                                            const SeqView& Q, const InTabs<typename S::Real>& T, int i,
+                                            int j) {
+    using R = typename S::Real;
+    const ParamView<R> P{tb->blob};
+    const int L = Q.L, m = T.m, d = j - i;
+    const R NEG = S::neg(), HALF = S::half();
+    const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
+    const bool fc_cell = (0 < i) && (j < L) && Q.pairable(i, j + 1);
+
+    // FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j]   (cpu.py:179-183)
+    R fm2 = NEG;
+    if (fm_region || fc_cell) {
+        int o1 = tri_off(1, m) + i;          // FM1[i][i+1]
+        int o2 = tri_off(d - 1, m) + i + 1;  // FM[i+1][j]
+        for (int k = i + 1; k < j; ++k) {
+            const R a = T.FM1[o1];
+            const R b = T.FM[o2];
+            if (a > HALF && b > HALF) fm2 = sr.plus(fm2, S::add(a, b));
+            const int s1 = k - i;            // span of FM1[i][k]
+            o1 += m - s1;                    // -> span s1 + 1
+            o2 += 1 - (m - (j - k - 1));     // FM[k+1][j]: span j-k-1, one position right
+        }
+    }
+
+    // FC[i][j], pair (i, j+1)   (cpu.py:185-230)
+    R fc = NEG;
+    if (fc_cell) {
+        const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
+        const R jB = tb->jB[idx4(si, sj1, si1, sj)];
+        R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
+        const int pmax = (i + CMAX < j) ? i + CMAX : j;
+        for (int p = i; p <= pmax; ++p) {
+            const int l1 = p - i;
+            int qmin = p + 2;
+            const int alt = l1 + j - CMAX;
+            if (alt > qmin) qmin = alt;
+            const int a = p + 1;
+            const int pca = Q.pc[a], sa = Q.s[a], sp = Q.s[p];
+            for (int q = j; q >= qmin; --q) {
+                if (!pairable_codes(pca, Q.pc[q])) continue;
+                const R inner = T.FC[tri_off(q - 1 - a, m) + a];
+                if (!(inner > HALF)) continue;
+                const int l2 = j - q;
+                R e;
+                if (l1 == 0 && l2 == 0) {
+                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
+                } else {
+                    const int sq = Q.s[q];
+                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], sp)];
+                    R snuc = R(0);
+                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
+                }
+                acc = sr.plus(acc, S::add(e, inner));
+            }
+        }
+        if (fm2 > HALF) {
+            const R jA = junctionA<S>(P, L, Q, i, j);
+            acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));
+        }
+        fc = acc;
+    }
+    T.FC[T.at(i, j)] = fc;
+
+    // FM1[i][j]   (cpu.py:232-246)
+    R fm1 = NEG;
+    if (fm_region) {
+        R acc = NEG;
+        const R fin = T.FC[T.at(i + 1, j - 1)];
+        if (Q.pairable(i + 1, j) && fin > HALF) {
+            const R jAji = junctionA_rev<S>(P, L, Q, i, j);
+            acc = sr.plus(acc, S::add(S::add(S::add(fin, jAji), P.mp()), P.bp(Q.s[i + 1], Q.s[j])));
+        }
+        const R ext = T.FM1[T.at(i + 1, j)];
+        if (ext > HALF) acc = sr.plus(acc, S::add(ext, P.mu()));
+        fm1 = acc;
+    }
+    T.FM1[T.at(i, j)] = fm1;
+
+    // FM[i][j]   (cpu.py:248-257)
+    R fm = NEG;
+    if (fm_region) {
+        R acc = NEG;
+        if (fm2 > HALF) acc = sr.plus(acc, fm2);
+        const R prev = T.FM[T.at(i, j - 1)];
+        if (prev > HALF) acc = sr.plus(acc, S::add(prev, P.mu()));
+        if (fm1 > HALF) acc = sr.plus(acc, fm1);
+        fm = acc;
+    }
+    T.FM[T.at(i, j)] = fm;
+}
+
+// Exterior recurrence F5 (cpu.py:259-274) by one warp.  F5[j] is a sequential
+// chain over k; the lanes evaluate 32 candidate terms at a time and every lane
+// then folds them in k order (warp-uniform), so the chain is the reference's.
+template <class S>
+__device__ __forceinline__ void exterior_warp(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
+                                              const SeqView& Q, const InTabs<typename S::Real>& T) {
+    using R = typename S::Real;
+    const ParamView<R> P{tb->blob};
+    const int L = Q.L, lane = threadIdx.x & 31;
+    const R HALF = S::half();
+    R f5prev = R(0);
+    if (lane == 0) T.F5[0] = R(0);
+    for (int j = 1; j <= L; ++j) {
+        R acc = S::add(f5prev, P.eu());
+        for (int k0 = 0; k0 < j; k0 += 32) {
+            const int k = k0 + lane;
+            bool ok = false;
+            R term = R(0);
+            if (k < j && Q.pairable(k + 1, j)) {
+                const R fcin = T.FC[T.at(k + 1, j - 1)];
+                const R f5k = T.F5[k];
+                if (fcin > HALF && f5k > HALF) {
+                    const R jA = junctionA_rev<S>(P, L, Q, k, j);
+                    term = S::add(S::add(S::add(S::add(f5k, fcin), P.ep()), P.bp(Q.s[k + 1], Q.s[j])), jA);
+                    ok = true;
+                }
+            }
+            unsigned mask = __ballot_sync(0xffffffffu, ok);
+            while (mask) {
+                const int t = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const R v = __shfl_sync(0xffffffffu, term, t);
+                acc = sr.plus(acc, v);
+            }
+        }
+        if (lane == 0) T.F5[j] = acc;
+        f5prev = acc;
+        __syncwarp();
+    }
+}
+
+}  // namespace cf

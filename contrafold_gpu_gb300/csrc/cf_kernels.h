@@ -1,0 +1,41 @@
+// cf_kernels.h -- kernel entry points and launch arguments (host + device).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "cf_device.cuh"
+
+namespace cf {
+
+constexpr int kFoldThreads = 256;   // threads per fold CTA
+constexpr int kMaxGroup = 32;       // sequences per CTA on the batched path
+
+struct FoldArgs {
+    const SeqDesc* descs;      // [n], grouped: CTA b owns descs[b*group .. b*group+group)
+    int n;
+    int group;
+    const uint8_t* seqs;       // ASCII
+    const uint8_t* mask;       // nullable
+    const float* blob32;
+    const double* blob64;
+    float* ws;                 // arena base
+    float* logz;               // [batch] or null
+    double* logz64;            // [batch] or null
+    char* structs;             // dot-brackets at seq_off
+    float* post_out;           // dense L*L per sequence or null
+    const int64_t* post_offs;  // indexed by SeqDesc::idx
+    float gamma;
+    int* status;               // device status word (CF_OK or an error code)
+};
+
+__global__ void k_inside32(FoldArgs A);
+__global__ void k_inside64(FoldArgs A);
+__global__ void k_outside32(FoldArgs A);
+__global__ void k_posterior32(FoldArgs A);
+__global__ void k_mea32(FoldArgs A);
+__global__ void k_viterbi64(FoldArgs A);
+
+size_t fold_smem_bytes(int Lmax, int group, bool fp64);
+
+}  // namespace cf

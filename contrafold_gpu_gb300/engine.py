@@ -1,0 +1,231 @@
+"""ctypes binding of the CUDA engine (libcontrafold_gb300.so, include/contrafold_gb300.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+usable, every call raises `EngineError`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import params as _params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcontrafold_gb300.so")
+
+CF_OK, CF_EINVAL, CF_ENOMEM, CF_ETIMEOUT, CF_ECUDA, CF_EDEVICE = 0, 1, 2, 3, 4, 5
+CF_MAX_LEN = 32767
+_STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "device wait timed out",
+           4: "CUDA error", 5: "device-side limit"}
+
+# Exported symbols of include/contrafold_gb300.h
+SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
+           "cf_engine_set_mode", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
+           "cf_mea", "cf_mfe", "cf_sample")
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{_STATUS.get(code, code)}] {msg}")
+        self.code = code
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load_library(path: str = LIB_PATH):
+    """dlopen the engine library (raises if it has not been built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise EngineError(CF_ECUDA, f"engine library not built: {path} (run contrafold_gpu_gb300.build.build())")
+        L = ctypes.CDLL(path)
+        P = ctypes.POINTER
+        vp, u8p, i64p = ctypes.c_void_p, P(ctypes.c_uint8), P(ctypes.c_int64)
+        f32p, f64p = P(ctypes.c_float), P(ctypes.c_double)
+        L.cf_engine_create.argtypes = [f32p, f64p, ctypes.c_int, P(vp)]
+        L.cf_engine_destroy.argtypes = [vp]
+        L.cf_engine_set_params.argtypes = [vp, f32p, f64p]
+        L.cf_engine_set_budget.argtypes = [vp, ctypes.c_size_t]
+        L.cf_engine_set_mode.argtypes = [vp, ctypes.c_int]
+        L.cf_last_error.restype = ctypes.c_char_p
+        L.cf_version.restype = ctypes.c_char_p
+        L.cf_logz.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f32p]
+        L.cf_logz64.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f64p]
+        L.cf_bpp.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, i64p, f32p, f32p]
+        L.cf_mea.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_float, ctypes.c_char_p]
+        L.cf_mfe.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_char_p]
+        if hasattr(L, "cf_sample"):
+            L.cf_sample.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
+                                    ctypes.c_char_p]
+        for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
+                     "cf_engine_set_mode", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe"):
+            getattr(L, name).restype = ctypes.c_int
+        if hasattr(L, "cf_sample"):
+            L.cf_sample.restype = ctypes.c_int
+        _lib = L
+        return L
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
+
+
+class Batch:
+    """A batch of sequences packed for the C-ABI: ASCII bytes, int64 offsets,
+    optional mask bytes (1 = forced unpaired).  Masks follow the reference:
+    None means unconstrained, longer masks are truncated (gpu.py:494)."""
+
+    def __init__(self, seqs: Sequence[str], masks: Optional[Sequence] = None):
+        self.seqs = [str(s) for s in seqs]
+        self.n = len(self.seqs)
+        lens = np.fromiter((len(s) for s in self.seqs), np.int64, self.n)
+        if self.n and lens.max() > CF_MAX_LEN:
+            raise ValueError(f"sequence longer than {CF_MAX_LEN} nt")
+        self.lens = lens
+        self.offsets = np.zeros(self.n + 1, np.int64)
+        np.cumsum(lens, out=self.offsets[1:])
+        self.total = int(self.offsets[-1])
+        self.buf = np.frombuffer("".join(self.seqs).encode("ascii", errors="replace"), np.uint8)
+        if self.buf.size != self.total:      # non-ASCII characters: encode per character
+            self.buf = np.array([ord(c) if ord(c) < 128 else ord("N") for c in "".join(self.seqs)], np.uint8)
+        self.mask = None
+        if masks is not None and any(m is not None for m in masks):
+            if len(masks) != self.n:
+                raise ValueError("one mask (or None) per sequence is required")
+            mk = np.zeros(max(self.total, 1), np.uint8)
+            for b, m in enumerate(masks):
+                if m is None:
+                    continue
+                L = int(lens[b])
+                arr = np.asarray(m).reshape(-1)
+                if arr.size < L:
+                    raise ValueError(f"mask of sequence {b} is shorter ({arr.size}) than the sequence ({L})")
+                mk[self.offsets[b]:self.offsets[b] + L] = (arr[:L] != 0)
+            self.mask = mk
+
+    def split_strings(self, raw: bytes, per: int = 1) -> List[str]:
+        s = raw.decode("ascii")
+        return [s[self.offsets[b] * per:self.offsets[b + 1] * per] for b in range(self.n)]
+
+
+class Engine:
+    """One device engine (parameters resident in HBM, a stream, a work arena)."""
+
+    def __init__(self, P: dict, device: int = 0, mode: str = "batched"):
+        self.lib = load_library()
+        self._h = ctypes.c_void_p()
+        b32, b64 = _params.pack32(P), _params.pack64(P)
+        self._check(self.lib.cf_engine_create(_p(b32, ctypes.c_float), _p(b64, ctypes.c_double), int(device),
+                                              ctypes.byref(self._h)))
+        self.device = device
+        self.set_mode(mode)
+        self._lock = threading.Lock()
+
+    def _check(self, rc):
+        if rc != CF_OK:
+            msg = self.lib.cf_last_error()
+            raise EngineError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.cf_engine_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, P: dict):
+        b32, b64 = _params.pack32(P), _params.pack64(P)
+        self._check(self.lib.cf_engine_set_params(self._h, _p(b32, ctypes.c_float), _p(b64, ctypes.c_double)))
+
+    def set_mode(self, mode: str):
+        self._check(self.lib.cf_engine_set_mode(self._h, {"plain": 0, "batched": 1}[mode]))
+        self.mode = mode
+
+    def set_budget(self, nbytes: int):
+        self._check(self.lib.cf_engine_set_budget(self._h, int(nbytes)))
+
+    # ---- batch entry points ----
+    def _args(self, B: Batch):
+        return (self._h, _p(B.buf, ctypes.c_uint8) if B.total else None, _p(B.offsets, ctypes.c_int64),
+                _p(B.mask, ctypes.c_uint8), ctypes.c_int32(B.n))
+
+    def logz(self, B: Batch) -> np.ndarray:
+        out = np.zeros(max(B.n, 1), np.float32)
+        with self._lock:
+            self._check(self.lib.cf_logz(*self._args(B), _p(out, ctypes.c_float)))
+        return out[:B.n]
+
+    def logz64(self, B: Batch) -> np.ndarray:
+        out = np.zeros(max(B.n, 1), np.float64)
+        with self._lock:
+            self._check(self.lib.cf_logz64(*self._args(B), _p(out, ctypes.c_double)))
+        return out[:B.n]
+
+    def bpp(self, B: Batch):
+        """Returns (list of float32 (L, L) matrices, float32 logZ array)."""
+        sq = B.lens * B.lens
+        po = np.zeros(B.n + 1, np.int64)
+        np.cumsum(sq, out=po[1:])
+        post = np.zeros(max(int(po[-1]), 1), np.float32)
+        z = np.zeros(max(B.n, 1), np.float32)
+        with self._lock:
+            self._check(self.lib.cf_bpp(*self._args(B), _p(po, ctypes.c_int64), _p(post, ctypes.c_float),
+                                        _p(z, ctypes.c_float)))
+        mats = [post[po[b]:po[b + 1]].reshape(int(B.lens[b]), int(B.lens[b])) for b in range(B.n)]
+        return mats, z[:B.n]
+
+    def mea(self, B: Batch, gamma: float = 6.0) -> List[str]:
+        out = ctypes.create_string_buffer(max(B.total, 1))
+        with self._lock:
+            self._check(self.lib.cf_mea(*self._args(B), ctypes.c_float(float(np.float32(gamma))), out))
+        return B.split_strings(out.raw[:B.total])
+
+    def mfe(self, B: Batch) -> List[str]:
+        out = ctypes.create_string_buffer(max(B.total, 1))
+        with self._lock:
+            self._check(self.lib.cf_mfe(*self._args(B), out))
+        return B.split_strings(out.raw[:B.total])
+
+    def sample(self, B: Batch, n_samples: int, seed: int = 0) -> List[List[str]]:
+        if n_samples < 0:
+            raise ValueError("n_samples must be >= 0")
+        out = ctypes.create_string_buffer(max(B.total * n_samples, 1))
+        with self._lock:
+            self._check(self.lib.cf_sample(*self._args(B), ctypes.c_int32(n_samples),
+                                           ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
+        raw = out.raw[:B.total * n_samples].decode("ascii")
+        res = []
+        for b in range(B.n):
+            L = int(B.lens[b])
+            base = int(B.offsets[b]) * n_samples
+            res.append([raw[base + t * L: base + (t + 1) * L] for t in range(n_samples)])
+        return res
+
+
+_engines = {}
+_engines_lock = threading.Lock()
+
+
+def engine_for(P: dict, device: int = 0) -> Engine:
+    """The engine bound to parameter dict P (created on first use, cached in P)."""
+    key = ("_engine", device)
+    eng = P.get(key) if isinstance(P, dict) else None
+    if eng is None:
+        with _engines_lock:
+            eng = P.get(key)
+            if eng is None:
+                eng = Engine(P, device)
+                P[key] = eng
+    return eng

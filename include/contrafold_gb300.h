@@ -1,0 +1,133 @@
+/*
+ * contrafold_gb300.h -- C-ABI of the GB300 (sm_103a) CONTRAfold folding engine.
+ *
+ * The engine replaces, behind a plain C interface, the compute entry points of
+ * the reference package `gpu_contrafold`:
+ *
+ *   cf_logz      <- gpu_contrafold/gpu.py:480-517   logZ_batch   (FP32 inside)
+ *   cf_logz64    <- gpu_contrafold/cpu.py:165-287   inside/logZ  (FP64 exact log1p/exp)
+ *   cf_bpp       <- gpu_contrafold/cpu.py:583-820,926-929  posterior/bpp
+ *   cf_mea       <- gpu_contrafold/cpu.py:823-895,932-941  mea_decode/mea
+ *   cf_mfe       <- gpu_contrafold/cpu.py:290-519   viterbi/mfe
+ *   cf_sample    <- gpu_contrafold/gpu.py:196-477,520-583  sample_kernel/sample_batch
+ *
+ * Conventions shared by every entry point
+ * ---------------------------------------
+ * - A batch of n sequences is one byte buffer `seqs` (ASCII, any case; A C G U,
+ *   T == U, any other byte is the unknown base N which never pairs and scores 0)
+ *   plus `offsets[n+1]` (int64, offsets[0] == 0, sequence b is
+ *   seqs[offsets[b] .. offsets[b+1])).
+ * - `mask` is NULL (no constraint) or a byte buffer laid out like `seqs`:
+ *   mask[offsets[b] + t] != 0 forces position t (0-based) of sequence b unpaired.
+ * - Per-sequence string outputs (dot-brackets) use the same offsets: sequence b
+ *   writes exactly L_b bytes '(' ')' '.' at out[offsets[b]]; no terminator.
+ * - Every call returns a status (CF_OK == 0).  On failure cf_last_error()
+ *   returns a thread-local, human-readable message.
+ * - Host-buffer calls are synchronous.  One engine must not be used from two
+ *   threads at once (one engine per host thread / stream).
+ */
+#ifndef CONTRAFOLD_GB300_H
+#define CONTRAFOLD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define CF_OK        0
+#define CF_EINVAL    1   /* bad argument (NULL pointer, bad length, bad gamma ...) */
+#define CF_ENOMEM    2   /* device allocation failed or over the engine's memory budget */
+#define CF_ETIMEOUT  3   /* a bounded device-side wait expired; the context stays usable */
+#define CF_ECUDA     4   /* CUDA runtime error */
+#define CF_EDEVICE   5   /* a kernel reported an internal limit (e.g. traceback stack) */
+
+/* Longest sequence accepted (partner indices are stored as int16 in the
+ * reference's sampler, gpu.py:559; the same bound is kept). */
+#define CF_MAX_LEN 32767
+
+/* ---- parameter blob layout (entries, float32 or float64) ----
+ * The blob is the concatenation of the tied tables produced by the loader
+ * (gpu_contrafold/cpu.py:40-135), each flattened in C order:
+ *   bp[5][5] stack[5][5][5][5] tm[5][5][5][5] hc[5][5] dl[5][5][5] dr[5][5][5]
+ *   hp_cum[31] cs[31][31] i11[5][5] b01[5] mb mu mp eu ep                        */
+#define CF_OFF_BP      0
+#define CF_OFF_STACK   25
+#define CF_OFF_TM      650
+#define CF_OFF_HC      1275
+#define CF_OFF_DL      1300
+#define CF_OFF_DR      1425
+#define CF_OFF_HPCUM   1550
+#define CF_OFF_CS      1581
+#define CF_OFF_I11     2542
+#define CF_OFF_B01     2567
+#define CF_OFF_MB      2572
+#define CF_OFF_MU      2573
+#define CF_OFF_MP      2574
+#define CF_OFF_EU      2575
+#define CF_OFF_EP      2576
+#define CF_BLOB_LEN    2577
+
+typedef struct cf_engine cf_engine;
+
+/* Create an engine on CUDA device `device` from the float32 and float64 blobs
+ * (both CF_BLOB_LEN entries).  The float32 blob drives every FP32 path; the
+ * float64 blob drives cf_logz64 and cf_mfe (the reference computes those in
+ * float64).  Replaces the per-call parameter upload of gpu.py:500-514. */
+int cf_engine_create(const float* params32, const double* params64, int device,
+                     cf_engine** out);
+int cf_engine_destroy(cf_engine* eng);
+/* Replace the parameter tables of an existing engine (e.g. after a gradient step). */
+int cf_engine_set_params(cf_engine* eng, const float* params32, const double* params64);
+/* Upper bound, in bytes, on the device work arena (0 = unlimited).  Batches
+ * larger than the budget are processed in slices; a single sequence that does
+ * not fit returns CF_ENOMEM. */
+int cf_engine_set_budget(cf_engine* eng, size_t bytes);
+/* Select the scheduling of the FP32 fold kernels: 0 = plain (one CTA per
+ * sequence, the reference's gpu.py:508 launch shape), 1 = batched (length-
+ * bucketed groups, autotuned group size).  Results are identical. */
+int cf_engine_set_mode(cf_engine* eng, int mode);
+
+const char* cf_last_error(void);
+const char* cf_version(void);
+
+/* log partition function, FP32 (Fast_LogPlusEquals arithmetic, like
+ * gpu.py:55-184).  logz_out[n]. */
+int cf_logz(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+            const uint8_t* mask, int32_t n, float* logz_out);
+
+/* log partition function, FP64 with exact log1p/exp (cpu.py:154-275). */
+int cf_logz64(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+              const uint8_t* mask, int32_t n, double* logz_out);
+
+/* Base-pair posterior matrices (cpu.py:583-820).  Sequence b writes L_b*L_b
+ * float32 values (row-major, 0-based, upper triangle; diagonal and lower
+ * triangle are 0) at post_out[post_offsets[b]].  logz_out (may be NULL)
+ * receives the FP32 logZ. */
+int cf_bpp(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+           const uint8_t* mask, int32_t n, const int64_t* post_offsets,
+           float* post_out, float* logz_out);
+
+/* Maximum-expected-accuracy structures (cpu.py:823-895): inside, outside,
+ * posterior and the gamma-weighted decode, all on the device. */
+int cf_mea(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+           const uint8_t* mask, int32_t n, float gamma, char* struct_out);
+
+/* Viterbi (maximum-probability) structures with the reference's first-match
+ * EPS=1e-6 traceback (cpu.py:290-519), in float64. */
+int cf_mfe(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+           const uint8_t* mask, int32_t n, char* struct_out);
+
+/* Boltzmann samples (stochastic traceback, gpu.py:196-477) with Philox4x32-10
+ * streams keyed by (seed, sequence index, sample index).  Sequence b writes
+ * n_samples * L_b bytes at out[offsets[b] * n_samples] (sample-major). */
+int cf_sample(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+              const uint8_t* mask, int32_t n, int32_t n_samples, uint64_t seed,
+              char* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CONTRAFOLD_GB300_H */

@@ -1,0 +1,208 @@
+"""Generate the golden fixtures from the reference engine itself.
+
+Imports the reference's CPU engine (gpu_contrafold/cpu.py, read from the
+reference checkout given by --ref, default /root/reference) under an identity
+`numba.njit` stub -- numba is not installed here, so the reference runs as
+plain Python/numpy with the same float32/float64 scalar semantics -- and
+records, for seeded inputs:
+
+  * the tied float64 parameter blob (cpu.load, cpu.py:40-135);
+  * FP64 logZ from cpu.inside (cpu.py:165-275), masks included;
+  * Viterbi structures from cpu.mfe (cpu.py:505-519);
+  * MEA structures from cpu.mea at several gammas (cpu.py:932-941);
+  * the FP32 posterior matrix from cpu.posterior (cpu.py:583-820): the full
+    bytes for short sequences, a SHA-256 of the float32 bytes for the rest;
+  * the reference's own literal known answers (GGGGAAAACCCC, README.md:101,104)
+    and the sequences of its validation script (tests/test_validation.py:15-27).
+
+Run once in a container that has the reference checkout:
+    python tests/golden/make_golden.py [--ref /root/reference] [--jobs 8]
+The output, tests/golden/golden.json (+ params_blob64.npy), is committed; the
+tests read only those files.
+"""
+from __future__ import annotations
+
+import argparse
+import base64
+import hashlib
+import importlib.util
+import json
+import multiprocessing as mp
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+_STUB = '''
+def njit(*args, **kwargs):
+    if len(args) == 1 and callable(args[0]) and not kwargs:
+        return args[0]
+    def deco(f):
+        return f
+    return deco
+'''
+
+_REF = None
+_P = None
+
+
+def load_reference(ref_root):
+    """Import <ref_root>/gpu_contrafold/cpu.py with an identity numba.njit."""
+    stub_dir = tempfile.mkdtemp(prefix="numba_stub_")
+    os.makedirs(os.path.join(stub_dir, "numba"))
+    with open(os.path.join(stub_dir, "numba", "__init__.py"), "w") as fh:
+        fh.write(_STUB)
+    sys.path.insert(0, stub_dir)
+    path = os.path.join(ref_root, "gpu_contrafold", "cpu.py")
+    spec = importlib.util.spec_from_file_location("ref_cpu", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _init(ref_root):
+    global _REF, _P
+    _REF = load_reference(ref_root)
+    _P = _REF.load()
+
+
+def _run_case(args):
+    seq, mask, gammas, want_post_bytes = args
+    R, P = _REF, _P
+    L = len(seq)
+    s, _ = R.encode(seq)
+    fo = np.zeros(L + 2, dtype=np.int64)
+    if mask is not None:
+        for k in range(L):
+            fo[k + 1] = int(mask[k])
+    t0 = time.time()
+    z64 = R.inside(s, L, fo, P["bp"], P["stack"], P["tm"], P["hc"], P["dl"], P["dr"],
+                   P["hp_cum"], P["cs"], P["i11"], P["b01"], P["mb"], P["mu"], P["mp"],
+                   P["eu"], P["ep"], R._CANON)
+    mfe = R.mfe(seq, P, mask)
+    _s, _L, _fo, POST = R._posterior(seq, P, mask)
+    f = R._params_f32(P)
+    meas = {}
+    for g in gammas:
+        pair = R.mea_decode(POST, L, _fo, R._CANON, _s, np.float32(g))
+        ch = ["."] * L
+        for t in range(1, L + 1):
+            if pair[t] > t:
+                ch[t - 1] = "("
+                ch[pair[t] - 1] = ")"
+        meas[repr(float(g))] = "".join(ch)
+    post = np.ascontiguousarray(POST, dtype=np.float32)
+    rec = {
+        "seq": seq,
+        "mask": None if mask is None else "".join("1" if int(x) else "0" for x in mask),
+        "logz64": float(z64),
+        "mfe": mfe,
+        "mea": meas,
+        "post_sha256": hashlib.sha256(post.tobytes()).hexdigest(),
+        "post_sum": float(post.astype(np.float64).sum()),
+        "seconds": round(time.time() - t0, 2),
+    }
+    if want_post_bytes:
+        rec["post_b64"] = base64.b64encode(post.tobytes()).decode("ascii")
+    del f
+    return rec
+
+
+def rand_seq(rng, L, alphabet="ACGU"):
+    return "".join(rng.choice(np.array(list(alphabet)), size=L))
+
+
+def build_cases():
+    cases = []
+    gam = [6.0]
+    gam_multi = [0.5, 1.0, 2.0, 4.0, 6.0, 8.0, 16.0]
+    # reference literal known answer (README.md:101,104)
+    cases.append(("GGGGAAAACCCC", None, gam_multi, True))
+    cases.append(("GCGCGCAAAAGCGCGCAAAAGCGC", None, gam_multi, True))
+    # edge cases: empty, tiny, non-ACGU, lowercase, T
+    for seq in ["", "A", "GC", "GAC", "GGGAAAUCC", "NNNNGGGGAAAACCCCNNNN", "ggggaaaacccc",
+                "GGGGTTTTCCCCAAAA", "ACGUXACGU-ACGU"]:
+        cases.append((seq, None, gam, True))
+    cases.append(("GGGGAAAACCCC", [0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0], gam, True))
+    cases.append(("GGGGAAAACCCC", [1] * 12, gam, True))
+    rng = np.random.default_rng(20260101)
+    # small random: lengths 4..60, half masked (Bernoulli 0.1 / 0.3), some N
+    for t in range(200):
+        L = int(rng.integers(4, 61))
+        alpha = "ACGU" if t % 7 else "ACGUN"
+        seq = rand_seq(rng, L, alpha)
+        mask = None
+        if t % 2 == 1:
+            p = 0.1 if t % 4 == 1 else 0.3
+            mask = (rng.random(L) < p).astype(np.int8).tolist()
+        cases.append((seq, mask, gam_multi if t % 10 == 0 else gam, t < 40))
+    # medium: 128 nt unmasked, 200 nt with Bernoulli(0.1) mask
+    for t in range(6):
+        cases.append((rand_seq(rng, 128), None, gam, False))
+    for t in range(4):
+        L = 200
+        seq = rand_seq(rng, L)
+        mask = (rng.random(L) < 0.1).astype(np.int8).tolist()
+        cases.append((seq, mask, [6.0, 2.0], False))
+    return cases
+
+
+def validation_script_sequences():
+    """Sequences drawn exactly as tests/test_validation.py:15-27 and :67-69 draw them."""
+    rng = np.random.default_rng(0)
+    bases = np.array(list("ACGU"))
+    seqs = ["".join(rng.choice(bases, size=int(rng.integers(30, 129)))) for _ in range(60)]
+    # check [4]: L=24 sequence and its Bernoulli(0.3) forced-unpaired mask
+    s4 = "".join(rng.choice(bases, size=24))
+    m4 = (rng.random(24) < 0.3).astype(np.int8).tolist()
+    return seqs, s4, m4
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--out", default=os.path.join(HERE, "golden.json"))
+    args = ap.parse_args()
+
+    R = load_reference(args.ref)
+    P = R.load()
+    sys.path.insert(0, REPO)
+    from contrafold_gpu_gb300 import params as prm
+    blob = prm.pack64(P)
+    np.save(os.path.join(HERE, "params_blob64.npy"), blob)
+
+    cases = build_cases()
+    val_seqs, s4, m4 = validation_script_sequences()
+    for sq in val_seqs[:20]:
+        cases.append((sq, None, [6.0], False))
+    cases.append((s4, m4, [6.0], True))
+
+    ctx = mp.get_context("spawn")
+    t0 = time.time()
+    with ctx.Pool(args.jobs, initializer=_init, initargs=(args.ref,)) as pool:
+        # longest first for load balance
+        order = sorted(range(len(cases)), key=lambda k: -len(cases[k][0]))
+        res = pool.map(_run_case, [cases[k] for k in order], chunksize=1)
+    recs = [None] * len(cases)
+    for k, r in zip(order, res):
+        recs[k] = r
+    out = {
+        "generator": "tests/golden/make_golden.py",
+        "reference": "gpu_contrafold/cpu.py (pure Python under an identity numba.njit)",
+        "params_blob64_sha256": hashlib.sha256(blob.tobytes()).hexdigest(),
+        "validation_script": {"seqs": val_seqs, "check4_seq": s4, "check4_mask": m4},
+        "cases": recs,
+    }
+    with open(args.out, "w") as fh:
+        json.dump(out, fh, indent=0)
+    print(f"wrote {len(recs)} cases to {args.out} in {time.time() - t0:.0f}s")
+
+
+if __name__ == "__main__":
+    main()

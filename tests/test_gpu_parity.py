@@ -1,0 +1,155 @@
+"""GPU parity: the CUDA engine (through the C-ABI) against the golden vectors of
+the reference and against the oracle on seeded batches.
+
+Tolerances (stated by the fold contract):
+  logZ FP32 vs FP64 oracle  <= 5e-4 absolute and <= 1e-4 relative
+  logZ FP32                 bitwise equal to the oracle's float32 inside (same operation order)
+  logZ FP64                 <= 1e-9 relative (CUDA vs glibc log1p/exp)
+  BPP                       bitwise equal to the reference float32 posterior (=> max-abs 0 <= 1e-4)
+  MEA / Viterbi             dot-brackets identical
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_post, mask_of
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(recs):
+    from contrafold_gpu_gb300.engine import Batch
+    return Batch([r["seq"] for r in recs], [mask_of(r) for r in recs])
+
+
+def _rand_batch(seed, n, lo, hi, p_mask=0.0, alphabet="ACGU"):
+    rng = np.random.default_rng(seed)
+    seqs, masks = [], []
+    al = np.array(list(alphabet))
+    for _ in range(n):
+        L = int(rng.integers(lo, hi + 1))
+        seqs.append("".join(rng.choice(al, size=L)))
+        masks.append((rng.random(L) < p_mask).astype(np.int8) if p_mask > 0 else None)
+    return seqs, masks
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_golden_logz64(engine, golden, mode):
+    engine.set_mode(mode)
+    recs = golden["cases"]
+    z = engine.logz64(_batch(recs))
+    for r, v in zip(recs, z):
+        assert abs(v - r["logz64"]) <= 1e-9 * max(1.0, abs(r["logz64"])), r["seq"]
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_golden_logz32_tolerance(engine, golden, mode):
+    engine.set_mode(mode)
+    recs = golden["cases"]
+    z = engine.logz(_batch(recs))
+    for r, v in zip(recs, z):
+        err = abs(float(v) - r["logz64"])
+        assert err <= 5e-4 and err <= 1e-4 * max(1.0, abs(r["logz64"])) + 1e-12 or err <= 1e-4, (r["seq"], err)
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_golden_bpp_bitwise(engine, golden, mode):
+    engine.set_mode(mode)
+    recs = golden["cases"]
+    mats, _ = engine.bpp(_batch(recs))
+    for r, M in zip(recs, mats):
+        L = len(r["seq"])
+        full = np.zeros((L + 2, L + 2), np.float32)
+        full[1:L + 1, 1:L + 1] = M
+        assert hashlib.sha256(full.tobytes()).hexdigest() == r["post_sha256"], r["seq"]
+        if "post_b64" in r:
+            ref = golden_post(r)[1:L + 1, 1:L + 1]
+            assert np.array_equal(ref.view(np.uint32), M.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_golden_mea(engine, golden, mode):
+    engine.set_mode(mode)
+    recs = golden["cases"]
+    gammas = sorted({g for r in recs for g in r["mea"]}, key=float)
+    for g in gammas:
+        sub = [r for r in recs if g in r["mea"]]
+        got = engine.mea(_batch(sub), float(g))
+        bad = [r["seq"] for r, s in zip(sub, got) if s != r["mea"][g]]
+        assert not bad, (g, bad[:3])
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_golden_mfe(engine, golden, mode):
+    engine.set_mode(mode)
+    recs = golden["cases"]
+    got = engine.mfe(_batch(recs))
+    bad = [r["seq"] for r, s in zip(recs, got) if s != r["mfe"]]
+    assert not bad, bad[:3]
+
+
+def test_random_batch_vs_oracle(engine, P, oracle):
+    """200 seeded sequences (20-150 nt, 10% mask): logZ FP32 bitwise vs the oracle's
+    float32 inside, BPP bitwise, MEA and Viterbi identical."""
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(11, 200, 20, 150, 0.1)
+    B = Batch(seqs, masks)
+    engine.set_mode("batched")
+    z = engine.logz(B)
+    mats, z2 = engine.bpp(B)
+    mea = engine.mea(B, 6.0)
+    mfe = engine.mfe(B)
+    zo = oracle.batch(oracle.JOB_LOGZ32, seqs, P, masks)
+    assert np.array_equal(np.float32(zo), z)
+    assert np.array_equal(z, z2)
+    assert mea == oracle.batch(oracle.JOB_MEA, seqs, P, masks, 6.0)
+    assert mfe == oracle.batch(oracle.JOB_MFE, seqs, P, masks)
+    for k in range(0, 200, 37):
+        L = len(seqs[k])
+        _, POST = oracle.posterior(seqs[k], P, masks[k])
+        assert np.array_equal(POST[1:L + 1, 1:L + 1].view(np.uint32), mats[k].view(np.uint32))
+
+
+def test_plain_equals_batched(engine):
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(5, 97, 1, 260, 0.1)
+    B = Batch(seqs, masks)
+    res = {}
+    for mode in ("plain", "batched"):
+        engine.set_mode(mode)
+        res[mode] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B))
+    assert np.array_equal(res["plain"][0], res["batched"][0])
+    assert res["plain"][1] == res["batched"][1]
+    assert res["plain"][2] == res["batched"][2]
+
+
+def test_edge_cases(engine, P, oracle):
+    from contrafold_gpu_gb300.engine import Batch
+    seqs = ["", "A", "GC", "NNNN", "GGGGAAAACCCC", "acgu" * 10, "GGGG" + "N" * 30 + "CCCC"]
+    B = Batch(seqs)
+    z = engine.logz64(B)
+    for s, v in zip(seqs, z):
+        assert abs(v - oracle.logz64(s, P)) <= 1e-9 * max(1.0, abs(v))
+    assert engine.mea(B, 6.0) == [oracle.mea(s, P) for s in seqs]
+    assert engine.mfe(B) == [oracle.mfe(s, P) for s in seqs]
+    # a fully forced sequence folds to all-unpaired with logZ = L * eu
+    Bf = Batch(["GGGGAAAACCCC"], [[1] * 12])
+    assert engine.mea(Bf, 6.0) == ["." * 12]
+    assert abs(engine.logz64(Bf)[0] - 12 * P["eu"]) < 1e-12
+
+
+def test_long_sequence_budget_slicing(engine, P, oracle):
+    """A small arena budget forces several slices; results are unchanged."""
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(7, 24, 100, 300, 0.1)
+    B = Batch(seqs, masks)
+    engine.set_mode("batched")
+    full = engine.mea(B, 6.0)
+    engine.set_budget(8 << 20)
+    try:
+        sliced = engine.mea(B, 6.0)
+    finally:
+        engine.set_budget(0)
+    assert full == sliced
+    assert full == oracle.batch(oracle.JOB_MEA, seqs, P, masks, 6.0)

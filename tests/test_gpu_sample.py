@@ -1,0 +1,89 @@
+"""Sampler checks: structure validity, forced-unpaired masks, reproducibility and
+pair frequencies against the posterior within 3 sigma binomial noise
+(the reference's own checks 3 and 4, tests/test_validation.py:44-76)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pairs(db):
+    st, out = [], []
+    for k, ch in enumerate(db):
+        if ch == "(":
+            st.append(k)
+        elif ch == ")":
+            out.append((st.pop(), k))
+    assert not st
+    return out
+
+
+def test_sample_valid_and_reproducible(engine, P):
+    from contrafold_gpu_gb300.engine import Batch
+    from contrafold_gpu_gb300.params import CODE
+    rng = np.random.default_rng(3)
+    seqs = ["".join(rng.choice(list("ACGU"), size=int(L))) for L in (12, 50, 133, 260)]
+    B = Batch(seqs)
+    a = engine.sample(B, 16, seed=7)
+    b = engine.sample(B, 16, seed=7)
+    c = engine.sample(B, 16, seed=8)
+    assert a == b
+    assert a != c
+    canon = {(0, 3), (3, 0), (1, 2), (2, 1), (2, 3), (3, 2)}
+    for s, ss in zip(seqs, a):
+        for db in ss:
+            assert len(db) == len(s)
+            for x, y in _pairs(db):
+                assert (CODE[s[x]], CODE[s[y]]) in canon
+
+
+def test_sample_forced_unpaired_mask(engine, golden):
+    """check [4] of the reference validation script: zero violations."""
+    from contrafold_gpu_gb300.engine import Batch
+    v = golden["validation_script"]
+    s4, m4 = v["check4_seq"], v["check4_mask"]
+    out = engine.sample(Batch([s4], [m4]), 2000, seed=2)[0]
+    viol = sum(1 for db in out for k, ch in enumerate(db) if m4[k] and ch != ".")
+    assert viol == 0
+
+
+@pytest.mark.parametrize("seq,n", [("GCGCGCAAAAGCGCGCAAAAGCGC", 20000)])
+def test_sample_frequencies_match_posterior(engine, P, oracle, seq, n):
+    """Pair frequencies vs posteriors: |f - p| <= 3 sqrt(p(1-p)/N) + 1/N for every pair."""
+    from contrafold_gpu_gb300.engine import Batch
+    L = len(seq)
+    out = engine.sample(Batch([seq]), n, seed=1)[0]
+    f = np.zeros((L, L))
+    for db in out:
+        for x, y in _pairs(db):
+            f[x, y] += 1
+    f /= n
+    p = oracle.bpp(seq, P)
+    tol = 3 * np.sqrt(p * (1 - p) / n) + 1.0 / n
+    assert np.all(np.abs(f - p) <= tol + 2e-4), np.max(np.abs(f - p) - tol)
+
+
+def test_sample_frequencies_random_masked(engine, P, oracle):
+    from contrafold_gpu_gb300.engine import Batch
+    rng = np.random.default_rng(17)
+    L, n = 60, 8000
+    seq = "".join(rng.choice(list("ACGU"), size=L))
+    mask = (rng.random(L) < 0.1).astype(np.int8)
+    out = engine.sample(Batch([seq], [mask]), n, seed=5)[0]
+    f = np.zeros((L, L))
+    for db in out:
+        for x, y in _pairs(db):
+            f[x, y] += 1
+    f /= n
+    p = oracle.bpp(seq, P, mask)
+    tol = 3.5 * np.sqrt(p * (1 - p) / n) + 1.0 / n
+    assert np.all(np.abs(f - p) <= tol + 2e-4), np.max(np.abs(f - p) - tol)
+
+
+def test_fold_tasks_gpu_api(P):
+    import contrafold_gpu_gb300 as cg
+    pytest.importorskip("torch")
+    seqs = ["GGGGAAAACCCC", "ACGUACGUAC", "GGGGAAAACCCCGGGGAAAACCCC"]
+    out = cg.fold_tasks_gpu(seqs, [None, [1] * 10, None], P, chunk=2, seed=3)
+    assert [len(s) for s in out] == [len(s) for s in seqs]
+    assert out[1] == "." * 10
