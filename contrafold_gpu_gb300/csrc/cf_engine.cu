@@ -191,7 +191,7 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     int dev_max = 0;
     CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device));
     if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");
-    const void* ks[] = {(const void*)cf::k_inside32, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
+    const void* ks[] = {(const void*)cf::k_inside32, (const void*)cf::k_inside32acc, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
                         (const void*)cf::k_posterior32, (const void*)cf::k_mea32, (const void*)cf::k_viterbi64};
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     eng->smem_optin = bytes;
@@ -244,7 +244,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, co
         const dim3 blk(cf::kFoldThreads);
         switch (job) {
             case JOB_LOGZ:
-                cf::k_inside32<<<grid, blk, smem, st>>>(A);
+                cf::k_inside32acc<<<grid, blk, smem, st>>>(A);
                 break;
             case JOB_LOGZ64:
                 cf::k_inside64<<<grid, blk, smem, st>>>(A);
@@ -270,7 +270,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, co
                 cf::k_viterbi64<<<grid, blk, smem, st>>>(A);
                 break;
             case JOB_SAMPLE: {
-                cf::k_inside32<<<grid, blk, smem, st>>>(A);
+                cf::k_inside32acc<<<grid, blk, smem, st>>>(A);
                 CF_CUDA(cudaGetLastError());
                 if (!sj || sj->n_samples <= 0) break;
                 cf::SampleArgs S;

@@ -122,6 +122,8 @@ __device__ __forceinline__ S make_sr(const PolyTables* pt);
 template <>
 __device__ __forceinline__ Lse32 make_sr<Lse32>(const PolyTables* pt) { return Lse32{pt}; }
 template <>
+__device__ __forceinline__ LseAcc32 make_sr<LseAcc32>(const PolyTables*) { return LseAcc32{}; }
+template <>
 __device__ __forceinline__ Lse64 make_sr<Lse64>(const PolyTables*) { return Lse64{}; }
 template <>
 __device__ __forceinline__ Max64 make_sr<Max64>(const PolyTables*) { return Max64{}; }
@@ -153,6 +155,19 @@ __global__ void __launch_bounds__(kFoldThreads) k_inside32(FoldArgs A) {
     if (A.logz != nullptr)
         for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
             const InTabs<float> T = in_tabs<Lse32>(A, sm->ws[g], sm->L[g]);
+            A.logz[sm->idx[g]] = T.F5[sm->L[g]];
+        }
+}
+
+// Same recurrence with accurate float32 log-sum-exp: logZ_batch and the sampler.
+__global__ void __launch_bounds__(kFoldThreads) k_inside32acc(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    const int stride = setup_group(sm, A, A.blob32);
+    inside_group<LseAcc32>(sm, A, stride);
+    if (A.logz != nullptr)
+        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
+            const InTabs<float> T = in_tabs<LseAcc32>(A, sm->ws[g], sm->L[g]);
             A.logz[sm->idx[g]] = T.F5[sm->L[g]];
         }
 }

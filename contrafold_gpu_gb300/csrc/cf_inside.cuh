@@ -25,6 +25,22 @@ struct Lse32 {
     __device__ __forceinline__ Real plus(Real acc, Real x) const { return lse32(pt, acc, x); }
 };
 
+// float32 log-sum-exp with accurate log1pf/expf.  Used where the result is
+// judged against the FP64 engine (logZ within 5e-4) rather than bitwise
+// against the reference's Fast_LogPlusEquals arithmetic.
+struct LseAcc32 {
+    using Real = float;
+    static __device__ __forceinline__ Real neg() { return CF_NEG32; }
+    static __device__ __forceinline__ Real half() { return CF_HALF32; }
+    static __device__ __forceinline__ Real add(Real a, Real b) { return __fadd_rn(a, b); }
+    __device__ __forceinline__ Real plus(Real acc, Real x) const {
+        if (acc < CF_HALF32) return x;
+        if (x < CF_HALF32) return acc;
+        const float hi = fmaxf(acc, x), lo = fminf(acc, x);
+        return __fadd_rn(hi, log1pf(expf(__fsub_rn(lo, hi))));
+    }
+};
+
 struct Lse64 {
     using Real = double;
     static __device__ __forceinline__ Real neg() { return CF_NEG64; }

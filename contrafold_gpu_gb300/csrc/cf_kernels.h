@@ -30,6 +30,7 @@ struct FoldArgs {
 };
 
 __global__ void k_inside32(FoldArgs A);
+__global__ void k_inside32acc(FoldArgs A);
 __global__ void k_inside64(FoldArgs A);
 __global__ void k_outside32(FoldArgs A);
 __global__ void k_posterior32(FoldArgs A);

@@ -93,8 +93,10 @@ int cf_engine_set_mode(cf_engine* eng, int mode);
 const char* cf_last_error(void);
 const char* cf_version(void);
 
-/* log partition function, FP32 (Fast_LogPlusEquals arithmetic, like
- * gpu.py:55-184).  logz_out[n]. */
+/* log partition function in FP32 (the recurrence of gpu.py:55-184) with an
+ * accurate float32 log-sum-exp (log1pf/expf), within 5e-4 of the FP64 engine.
+ * The reference's Fast_LogPlusEquals value (bitwise that of cpu.py:595-678)
+ * is what cf_bpp returns in logz_out.  logz_out[n]. */
 int cf_logz(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
             const uint8_t* mask, int32_t n, float* logz_out);
 
@@ -102,10 +104,11 @@ int cf_logz(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
 int cf_logz64(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
               const uint8_t* mask, int32_t n, double* logz_out);
 
-/* Base-pair posterior matrices (cpu.py:583-820).  Sequence b writes L_b*L_b
- * float32 values (row-major, 0-based, upper triangle; diagonal and lower
- * triangle are 0) at post_out[post_offsets[b]].  logz_out (may be NULL)
- * receives the FP32 logZ. */
+/* Base-pair posterior matrices (cpu.py:583-820), bitwise the reference's
+ * float32 posterior.  Sequence b writes L_b*L_b float32 values (row-major,
+ * 0-based, upper triangle; diagonal and lower triangle are 0) at
+ * post_out[post_offsets[b]].  logz_out (may be NULL) receives the
+ * Fast_LogPlusEquals logZ the posterior is normalised by. */
 int cf_bpp(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
            const uint8_t* mask, int32_t n, const int64_t* post_offsets,
            float* post_out, float* logz_out);
