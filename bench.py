@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Headline benchmark: 200-nt MEA folds/s on GB300.
+
+Workload (one step): 10,000 sequences x 200 nt, bases i.i.d. uniform ACGU
+(np.random.default_rng(0).integers(0, 4, (10000, 200))), forced-unpaired mask
+Bernoulli(0.1) (np.random.default_rng(1).random((10000, 200)) < 0.1), full MEA
+fold per sequence: FP32 inside, outside, posterior and the gamma = 6 decode
+with traceback (bitwise the reference's float32 engine).
+
+  value  : folds/s of the batched (length-bucketed) plan with inputs resident in
+           HBM, CUDA events around each step on the launch stream, L2 flushed
+           (256 MiB write) between steps, max over ranks.
+  plain  : the same with the plain one-sequence-per-CTA launch shape.
+  e2e    : folds/s through the public API (contrafold_gpu_gb300.gpu.mea_batch:
+           Python strings in, dot-brackets out; host->device and device->host
+           copies inside the timed region).
+  roofline : the dominant kernel's algorithmic FP32 operations (guarded
+           semiring updates counted exactly on a sample of the workload by the
+           oracle, scaled to the batch) / its CUDA-event time, against the FP32
+           issue peak (SMs x 128 lanes x max SM clock).
+  cpu_baseline : the oracle (C restatement of the reference's CPU engine) on
+           all host cores over a bounded sample of the same workload.
+
+`--impl reference` times the reference's CPU engine (the oracle port, all host
+threads) on the same workload, one bounded sample per step.
+
+Multi-GPU (torchrun): replicas, each rank folds its own 10,000-sequence batch
+(weak scaling); no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+with open(os.path.join(REPO, "BASELINE.json")) as _fh:
+    METRIC = json.load(_fh)["metric"]
+UNIT = "folds/s"
+
+
+def workload(n: int, L: int, p_mask: float = 0.1):
+    idx = np.random.default_rng(0).integers(0, 4, size=(n, L), dtype=np.int8)
+    seq_bytes = np.frombuffer(b"ACGU", np.uint8)[idx]                       # (n, L) ASCII
+    mask = (np.random.default_rng(1).random((n, L)) < p_mask).astype(np.uint8)
+    return seq_bytes, mask
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_dev{device}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(REPO, "profiles", "ncu_traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+# --------------------------------------------------------------------------- CPU baseline leg
+def cpu_baseline_leg(seq_bytes, mask, gpu_structs, budget_s: float = 12.0):
+    """Oracle (C restatement of the reference CPU engine) on all host cores over a
+    bounded sample of the workload; also the exact guarded-update counts of a
+    sample for the roofline and a structure cross-check of the GPU output."""
+    import contrafold_gpu_gb300 as cg
+    from oracle import oracle as O
+    O.build()
+    P = cg.load()
+    cores = os.cpu_count() or 1
+    n, L = seq_bytes.shape
+    seqs = [bytes(r).decode() for r in seq_bytes]
+    masks = [m for m in mask]
+    # exact op counts on 32 sequences of the workload
+    cnt = np.zeros(8, np.float64)
+    ns = min(32, n)
+    for b in range(ns):
+        cnt += O.count_mea_ops(seqs[b], P, masks[b], 6.0)
+    counts_per_fold = cnt / ns
+    # timed sample: grow in chunks of 4*cores until the budget is spent
+    done, t_total, match = 0, 0.0, True
+    chunk = max(16, 4 * cores)
+    while done < n and t_total < budget_s:
+        sl = slice(done, min(n, done + chunk))
+        t0 = time.perf_counter()
+        out = O.batch(O.JOB_MEA, seqs[sl], P, masks[sl], 6.0, threads=cores)
+        t_total += time.perf_counter() - t0
+        if gpu_structs is not None:
+            match &= out == gpu_structs[sl]
+        done = sl.stop
+    return {"value": done / t_total, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {done} sequences of the workload (MEA gamma=6, 200 nt, 10% mask), "
+                      f"{cores} threads, {t_total:.1f} s",
+            "structures_match_gpu": bool(match)}, counts_per_fold
+
+
+# --------------------------------------------------------------------------- reference arm
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import contrafold_gpu_gb300 as cg
+    from oracle import oracle as O
+    O.build()
+    P = cg.load()
+    cores = os.cpu_count() or 1
+    seq_bytes, mask = workload(args.n, args.L)
+    per = max(32, 4 * cores)
+    seqs = [bytes(r).decode() for r in seq_bytes[: per * (args.steps + args.warmup)]]
+    masks = list(mask[: per * (args.steps + args.warmup)])
+    for w in range(args.warmup):
+        O.batch(O.JOB_MEA, seqs[w * per:(w + 1) * per], P, masks[w * per:(w + 1) * per], 6.0, threads=cores)
+    t = 0.0
+    for k in range(args.steps):
+        o = (args.warmup + k) * per
+        t0 = time.perf_counter()
+        O.batch(O.JOB_MEA, seqs[o:o + per], P, masks[o:o + per], 6.0, threads=cores)
+        t += time.perf_counter() - t0
+    v = per * args.steps / t
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(args), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per} sequences of the workload per step, {cores} threads "
+                                       f"(C restatement of gpu_contrafold/cpu.py posterior + mea_decode)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config_dict(args):
+    return {"workload": f"MEA fold (inside+outside+posterior+gamma=6 decode), {args.n} x {args.L} nt i.i.d. ACGU, "
+                        f"Bernoulli(0.1) forced-unpaired mask",
+            "n_seqs": args.n, "seq_len": args.L, "gamma": 6.0, "mask_p": 0.1,
+            "l2": "flushed between steps (256 MiB write); arena per step exceeds L2",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# --------------------------------------------------------------------------- our arm
+def our_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import contrafold_gpu_gb300 as cg
+    from contrafold_gpu_gb300 import build as cbuild
+    from contrafold_gpu_gb300.engine import CF_JOB_MEA, CF_JOB_LOGZ, CF_JOB_LOGZ64, Engine, Plan
+    if rank == 0:
+        cbuild.build()
+    if dist is not None:
+        dist.barrier()
+    P = cg.load()
+    n, L = args.n, args.L
+    seq_bytes, mask = workload(n, L)
+    offsets = np.arange(n + 1, dtype=np.int64) * L
+    dev = torch.device("cuda", local)
+    d_seqs = torch.from_numpy(seq_bytes.reshape(-1).copy()).to(dev)
+    d_mask = torch.from_numpy(mask.reshape(-1).copy()).to(dev)
+    d_out = torch.empty(n * L, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def sync_all():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def run_mode(mode, timing=True):
+        eng = Engine(P, device=local, mode=mode)
+        plan = Plan(eng, CF_JOB_MEA, offsets)
+        plan.set_timing(timing)
+        for _ in range(args.warmup):
+            plan.run(d_seqs.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+        plan.status()
+        step_ms, phase = [], np.zeros(4)
+        for _ in range(args.steps):
+            flush.fill_(1)
+            sync_all()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(d_seqs.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+            e1.record(stream)
+            sync_all()
+            step_ms.append(e0.elapsed_time(e1))
+            if timing:
+                phase += plan.phase_ms()
+        plan.status()
+        res = {"step_ms": step_ms, "phase_ms": phase / args.steps, "launches": plan.launches * args.steps,
+               "group": plan.group, "arena_bytes": plan.arena_bytes}
+        plan.close()
+        eng.close()
+        return res
+
+    # plain launch shape first, then the batched path under the clock sampler
+    plain = run_mode("plain")
+    with ClockSampler(local) as clk:
+        batched = run_mode("batched")
+    clocks = clk.summary()
+    structs = d_out.cpu().numpy().reshape(n, L).tobytes().decode("ascii")
+    gpu_structs = [structs[b * L:(b + 1) * L] for b in range(n)]
+
+    def agg(total_ms):
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    t_b = agg(sum(batched["step_ms"]))
+    t_p = agg(sum(plain["step_ms"]))
+    value = n * args.steps * world / (t_b / 1000.0)
+    plain_value = n * args.steps * world / (t_p / 1000.0)
+
+    # e2e through the public API (strings in, structures out)
+    seq_strs = [bytes(r).decode() for r in seq_bytes]
+    masks = list(mask)
+    for _ in range(max(1, args.warmup // 2)):
+        cg.gpu.mea_batch(seq_strs, P, 6.0, masks)
+    sync_all()
+    t0 = time.perf_counter()
+    e2e_out = None
+    for _ in range(args.steps):
+        e2e_out = cg.gpu.mea_batch(seq_strs, P, 6.0, masks)
+    t_e2e = agg((time.perf_counter() - t0) * 1000.0)
+    e2e_value = n * args.steps * world / (t_e2e / 1000.0)
+    e2e_ok = e2e_out == gpu_structs
+
+    # logZ accuracy of the FP32 logZ path against the FP64 engine on 1,000 sequences
+    m = min(1000, n)
+    eng = Engine(P, device=local)
+    from contrafold_gpu_gb300.engine import Batch
+    Bz = Batch(seq_strs[:m], masks[:m])
+    logz_err = float(np.max(np.abs(eng.logz(Bz).astype(np.float64) - eng.logz64(Bz))))
+    eng.close()
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    cpu, counts = cpu_baseline_leg(seq_bytes, mask, gpu_structs)
+    from oracle.oracle import OP_COST
+    phase_cats = {0: (0, 1, 2), 1: (3, 4, 5), 2: (6,), 3: (7,)}
+    names = {0: "k_inside32", 1: "k_outside32", 2: "k_posterior32", 3: "k_mea32"}
+    ph = batched["phase_ms"]
+    dom = int(np.argmax(ph))
+    ops_per_fold = {k: float(sum(counts[c] * OP_COST[c] for c in cats)) for k, cats in phase_cats.items()}
+    achieved = ops_per_fold[dom] * n / (ph[dom] / 1000.0) / 1e12
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12
+    tr = ncu_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == names[dom]:
+        traffic = tr.get("bytes_per_launch_full")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_b / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
+        "plain": {"value": plain_value, "ms_per_step": t_p / args.steps, "group": plain["group"]},
+        "batched_group": batched["group"],
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(2 * n * L + 8 * (n + 1) + 24 * n),
+                "d2h_bytes_per_step": int(n * L + 4), "api": "contrafold_gpu_gb300.gpu.mea_batch",
+                "matches_device_path": bool(e2e_ok)},
+        "gpu_launches": int(batched["launches"]),
+        "roofline": {"bound": "fp32", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_note": f"{props.multi_processor_count} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz "
+                                  "(sm_max_mhz of MEASURED_PEAKS.json); the DP is a log/max semiring, "
+                                  "neither HBM- nor tensor-bound",
+                     "ops_per_fold": ops_per_fold[dom],
+                     "phase_ms": {names[k]: float(ph[k]) for k in range(4)}},
+        "ops_per_fold_total": float(sum(ops_per_fold.values())),
+        "logz_max_abs_err_fp32_vs_fp64": logz_err,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=10000)
+    ap.add_argument("--L", type=int, default=200)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

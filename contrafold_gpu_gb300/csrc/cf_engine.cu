@@ -198,26 +198,86 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     return CF_OK;
 }
 
-// Runs `job` over a batch whose inputs are already on the device.
+// Per-phase device timing with CUDA events (phases: 0 inside, 1 outside,
+// 2 posterior, 3 decode / traceback / sampling).
+constexpr int kPhases = 4;
+struct PhaseTimer {
+    bool on = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    size_t used = 0;
+    void reset() { used = 0; }
+    int begin(int phase, cudaStream_t st, cudaEvent_t* stop) {
+        if (!on) return CF_OK;
+        if (used == marks.size()) {
+            cudaEvent_t a, b;
+            CF_CUDA(cudaEventCreate(&a));
+            CF_CUDA(cudaEventCreate(&b));
+            marks.push_back({phase, {a, b}});
+        }
+        auto& m = marks[used++];
+        m.first = phase;
+        CF_CUDA(cudaEventRecord(m.second.first, st));
+        *stop = m.second.second;
+        return CF_OK;
+    }
+    int end(cudaEvent_t stop, cudaStream_t st) {
+        if (!on) return CF_OK;
+        CF_CUDA(cudaEventRecord(stop, st));
+        return CF_OK;
+    }
+    int read(float* ms, int nph) {
+        for (int k = 0; k < nph; ++k) ms[k] = 0.f;
+        for (size_t u = 0; u < used; ++u) {
+            float t = 0.f;
+            CF_CUDA(cudaEventSynchronize(marks[u].second.second));
+            CF_CUDA(cudaEventElapsedTime(&t, marks[u].second.first, marks[u].second.second));
+            if (marks[u].first < nph) ms[marks[u].first] += t;
+        }
+        return CF_OK;
+    }
+    ~PhaseTimer() {
+        for (auto& m : marks) {
+            cudaEventDestroy(m.second.first);
+            cudaEventDestroy(m.second.second);
+        }
+    }
+};
+
 struct SampleJob {
     int n_samples = 0;
     uint64_t seed = 0;
     char* d_out = nullptr;
 };
 
-int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, const uint8_t* d_mask, float gamma,
-               float* d_logz, double* d_logz64, char* d_structs, float* d_post, const int64_t* d_post_offs,
-               cudaStream_t st, const SampleJob* sj = nullptr) {
+// Device resources one execution uses: descriptors (already uploaded), arena,
+// status word, optional phase timer.
+struct Exec {
+    const SeqDesc* d_descs = nullptr;
+    float* arena = nullptr;
+    int* status = nullptr;
+    PhaseTimer* timer = nullptr;
+    int launches = 0;   // kernels launched by the last run
+};
+
+#define CF_PHASE(ph, launch)                                                \
+    do {                                                                   \
+        cudaEvent_t stop_ = nullptr;                                       \
+        if (X.timer && (rc = X.timer->begin((ph), st, &stop_))) return rc; \
+        launch;                                                            \
+        ++X.launches;                                                      \
+        CF_CUDA(cudaGetLastError());                                       \
+        if (X.timer && (rc = X.timer->end(stop_, st))) return rc;          \
+    } while (0)
+
+// Launches `job` over a planned batch whose inputs are already on the device.
+int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d_seqs, const uint8_t* d_mask,
+               float gamma, float* d_logz, double* d_logz64, char* d_structs, float* d_post,
+               const int64_t* d_post_offs, cudaStream_t st, const SampleJob* sj = nullptr) {
     const int n = (int)P.descs.size();
+    X.launches = 0;
+    if (X.timer) X.timer->reset();
     if (n == 0) return CF_OK;
-    int rc = eng->descs.ensure(n);
-    if (rc) return rc;
-    CF_CUDA(cudaMemcpyAsync(eng->descs.p, P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice, st));
-    int64_t maxw = 0;
-    for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
-    if ((rc = eng->arena.ensure((size_t)std::max<int64_t>(maxw, 1)))) return rc;
-    if ((rc = eng->status.ensure(1))) return rc;
-    CF_CUDA(cudaMemsetAsync(eng->status.p, 0, sizeof(int), st));
+    int rc;
     const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
     const size_t smem = cf::fold_smem_bytes(P.Lmax, P.group, fp64);
     if ((rc = ensure_smem(eng, smem))) return rc;
@@ -225,53 +285,52 @@ int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, co
     for (size_t s = 0; s + 1 < P.slice_begin.size(); ++s) {
         const int k0 = P.slice_begin[s], k1 = P.slice_begin[s + 1];
         cf::FoldArgs A;
-        A.descs = eng->descs.p + k0;
+        A.descs = X.d_descs + k0;
         A.n = k1 - k0;
         A.group = P.group;
         A.seqs = d_seqs;
         A.mask = d_mask;
         A.blob32 = eng->blob32.p;
         A.blob64 = eng->blob64.p;
-        A.ws = eng->arena.p;
+        A.ws = X.arena;
         A.logz = d_logz;
         A.logz64 = d_logz64;
         A.structs = d_structs;
         A.post_out = d_post;
         A.post_offs = d_post_offs;
         A.gamma = gamma;
-        A.status = eng->status.p;
+        A.status = X.status;
         const int grid = (A.n + P.group - 1) / P.group;
         const dim3 blk(cf::kFoldThreads);
         switch (job) {
             case JOB_LOGZ:
-                cf::k_inside32acc<<<grid, blk, smem, st>>>(A);
+                CF_PHASE(0, (cf::k_inside32acc<<<grid, blk, smem, st>>>(A)));
                 break;
             case JOB_LOGZ64:
-                cf::k_inside64<<<grid, blk, smem, st>>>(A);
+                CF_PHASE(0, (cf::k_inside64<<<grid, blk, smem, st>>>(A)));
                 break;
             case JOB_BPP:
             case JOB_MEA: {
                 cf::FoldArgs Ai = A;
                 Ai.logz = nullptr;
-                cf::k_inside32<<<grid, blk, smem, st>>>(Ai);
-                cf::k_outside32<<<grid, blk, smem, st>>>(A);
+                CF_PHASE(0, (cf::k_inside32<<<grid, blk, smem, st>>>(Ai)));
+                CF_PHASE(1, (cf::k_outside32<<<grid, blk, smem, st>>>(A)));
                 if (job == JOB_BPP) {
-                    cf::k_posterior32<<<grid, blk, smem, st>>>(A);
+                    CF_PHASE(2, (cf::k_posterior32<<<grid, blk, smem, st>>>(A)));
                 } else {
                     cf::FoldArgs Ap = A;
                     Ap.post_out = nullptr;
                     Ap.logz = nullptr;
-                    cf::k_posterior32<<<grid, blk, smem, st>>>(Ap);
-                    cf::k_mea32<<<grid, blk, smem, st>>>(A);
+                    CF_PHASE(2, (cf::k_posterior32<<<grid, blk, smem, st>>>(Ap)));
+                    CF_PHASE(3, (cf::k_mea32<<<grid, blk, smem, st>>>(A)));
                 }
                 break;
             }
             case JOB_MFE:
-                cf::k_viterbi64<<<grid, blk, smem, st>>>(A);
+                CF_PHASE(0, (cf::k_viterbi64<<<grid, blk, smem, st>>>(A)));
                 break;
             case JOB_SAMPLE: {
-                cf::k_inside32acc<<<grid, blk, smem, st>>>(A);
-                CF_CUDA(cudaGetLastError());
+                CF_PHASE(0, (cf::k_inside32acc<<<grid, blk, smem, st>>>(A)));
                 if (!sj || sj->n_samples <= 0) break;
                 cf::SampleArgs S;
                 S.descs = A.descs;
@@ -282,23 +341,22 @@ int run_device(cf_engine* eng, Job job, const Plan& P, const uint8_t* d_seqs, co
                 S.seqs = d_seqs;
                 S.mask = d_mask;
                 S.blob32 = eng->blob32.p;
-                S.ws = eng->arena.p;
+                S.ws = X.arena;
                 S.out = sj->d_out;
-                S.status = eng->status.p;
+                S.status = X.status;
                 const size_t ssm = cf::sample_smem_bytes(P.Lmax);
                 if (ssm > 48 * 1024)
                     CF_CUDA(cudaFuncSetAttribute((const void*)cf::k_sample32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)ssm));
                 const int64_t items = (int64_t)A.n * sj->n_samples;
                 const int warps = cf::sample_threads() / 32;
-                int sgrid = (int)std::min<int64_t>((items + warps - 1) / warps, 152 * 16);
-                cf::k_sample32<<<sgrid, cf::sample_threads(), ssm, st>>>(S);
+                const int sgrid = (int)std::min<int64_t>((items + warps - 1) / warps, 152 * 16);
+                CF_PHASE(3, (cf::k_sample32<<<sgrid, cf::sample_threads(), ssm, st>>>(S)));
                 break;
             }
             default:
                 return fail(CF_EINVAL, "bad job");
         }
-        CF_CUDA(cudaGetLastError());
     }
     return CF_OK;
 }
@@ -370,8 +428,19 @@ int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offset
         sj.seed = seed;
         sj.d_out = eng->samples.p;
     }
-    if ((rc = run_device(eng, job, P, eng->seqs.p, d_mask, gamma, d_logz, d_logz64, d_structs, d_post, d_post_offs, st,
-                         &sj)))
+    if ((rc = eng->descs.ensure(n))) return rc;
+    CF_CUDA(cudaMemcpyAsync(eng->descs.p, P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice, st));
+    int64_t maxw = 1;
+    for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
+    if ((rc = eng->arena.ensure((size_t)maxw))) return rc;
+    if ((rc = eng->status.ensure(1))) return rc;
+    CF_CUDA(cudaMemsetAsync(eng->status.p, 0, sizeof(int), st));
+    Exec X;
+    X.d_descs = eng->descs.p;
+    X.arena = eng->arena.p;
+    X.status = eng->status.p;
+    if ((rc = run_device(eng, job, P, X, eng->seqs.p, d_mask, gamma, d_logz, d_logz64, d_structs, d_post, d_post_offs,
+                         st, &sj)))
         return rc;
     if (sample_out && sample_bytes)
         CF_CUDA(cudaMemcpyAsync(sample_out, sj.d_out, sample_bytes, cudaMemcpyDeviceToHost, st));
@@ -488,5 +557,105 @@ int cf_sample(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const u
     return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, n_samples,
                     seed, out);
 }
+
+}  // extern "C"
+
+// ============================ plans (device-resident batches) ============================
+struct cf_plan {
+    cf_engine* eng = nullptr;
+    Job job = JOB_MEA;
+    Plan P;
+    int n = 0;
+    DevBuf<SeqDesc> descs;
+    DevBuf<float> arena;
+    DevBuf<int> status;
+    PhaseTimer timer;
+    int launches = 0;
+};
+
+extern "C" {
+
+int cf_plan_create(cf_engine* e, int32_t job, const int64_t* offsets, int32_t n, cf_plan** out) {
+    if (!out) return fail(CF_EINVAL, "out is NULL");
+    *out = nullptr;
+    int rc = check_batch(e, reinterpret_cast<const uint8_t*>(1), offsets, n);
+    if (rc) return rc;
+    if (job != CF_JOB_LOGZ && job != CF_JOB_LOGZ64 && job != CF_JOB_MEA && job != CF_JOB_MFE)
+        return fail(CF_EINVAL, "plans support CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE");
+    CF_CUDA(cudaSetDevice(e->device));
+    cf_plan* p = new cf_plan();
+    p->eng = e;
+    p->job = job == CF_JOB_LOGZ ? JOB_LOGZ : job == CF_JOB_LOGZ64 ? JOB_LOGZ64 : job == CF_JOB_MEA ? JOB_MEA : JOB_MFE;
+    p->n = n;
+    if ((rc = make_plan(e, p->job, offsets, n, p->P)) || (rc = p->descs.ensure(std::max(n, 1))) ||
+        (rc = p->status.ensure(1))) {
+        delete p;
+        return rc;
+    }
+    int64_t maxw = 1;
+    for (int64_t w : p->P.slice_words) maxw = std::max(maxw, w);
+    if ((rc = p->arena.ensure((size_t)maxw))) {
+        p->descs.release(); p->status.release();
+        delete p;
+        return rc;
+    }
+    if (n) CF_CUDA(cudaMemcpy(p->descs.p, p->P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice));
+    CF_CUDA(cudaMemset(p->status.p, 0, sizeof(int)));
+    *out = p;
+    return CF_OK;
+}
+
+int cf_plan_destroy(cf_plan* p) {
+    if (!p) return CF_OK;
+    cudaSetDevice(p->eng->device);
+    cudaDeviceSynchronize();
+    p->descs.release(); p->arena.release(); p->status.release();
+    delete p;
+    return CF_OK;
+}
+
+size_t cf_plan_arena_bytes(const cf_plan* p) { return p ? p->arena.cap * sizeof(float) : 0; }
+
+int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float gamma, void* d_out, void* stream) {
+    if (!p) return fail(CF_EINVAL, "plan is NULL");
+    if (p->n > 0 && (!d_out || (!d_seqs && p->P.Lmax > 0))) return fail(CF_EINVAL, "NULL device buffer");
+    if (p->job == JOB_MEA && !(gamma > 0.0f)) return fail(CF_EINVAL, "gamma must be > 0");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : p->eng->stream;
+    Exec X;
+    X.d_descs = p->descs.p;
+    X.arena = p->arena.p;
+    X.status = p->status.p;
+    X.timer = p->timer.on ? &p->timer : nullptr;
+    float* lz = p->job == JOB_LOGZ ? static_cast<float*>(d_out) : nullptr;
+    double* lz64 = p->job == JOB_LOGZ64 ? static_cast<double*>(d_out) : nullptr;
+    char* st_out = (p->job == JOB_MEA || p->job == JOB_MFE) ? static_cast<char*>(d_out) : nullptr;
+    int rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
+    p->launches = X.launches;
+    return rc;
+}
+
+int cf_plan_status(cf_plan* p) {
+    if (!p) return fail(CF_EINVAL, "plan is NULL");
+    int h = 0;
+    CF_CUDA(cudaMemcpy(&h, p->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h != CF_OK) return fail(h, "a kernel reported an internal limit (traceback stack/queue)");
+    return CF_OK;
+}
+
+int cf_plan_set_timing(cf_plan* p, int on) {
+    if (!p) return fail(CF_EINVAL, "plan is NULL");
+    p->timer.on = on != 0;
+    return CF_OK;
+}
+
+int cf_plan_phase_ms(cf_plan* p, float* ms, int32_t nphases) {
+    if (!p || !ms) return fail(CF_EINVAL, "NULL argument");
+    if (!p->timer.on) return fail(CF_EINVAL, "timing is off for this plan");
+    return p->timer.read(ms, std::min<int32_t>(nphases, kPhases));
+}
+
+int cf_plan_launches(const cf_plan* p) { return p ? p->launches : 0; }
+
+int cf_plan_group(const cf_plan* p) { return p ? p->P.group : 0; }
 
 }  // extern "C"

@@ -25,7 +25,10 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
            "cf_engine_set_mode", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
-           "cf_mea", "cf_mfe", "cf_sample")
+           "cf_mea", "cf_mfe", "cf_sample", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
+           "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
+           "cf_plan_group")
+CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE = 0, 1, 3, 4
 
 
 class EngineError(RuntimeError):
@@ -62,14 +65,23 @@ def load_library(path: str = LIB_PATH):
         L.cf_bpp.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, i64p, f32p, f32p]
         L.cf_mea.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_float, ctypes.c_char_p]
         L.cf_mfe.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_char_p]
-        if hasattr(L, "cf_sample"):
-            L.cf_sample.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
-                                    ctypes.c_char_p]
+        L.cf_sample.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
+                                ctypes.c_char_p]
+        L.cf_plan_create.argtypes = [vp, ctypes.c_int32, i64p, ctypes.c_int32, P(vp)]
+        L.cf_plan_destroy.argtypes = [vp]
+        L.cf_plan_arena_bytes.argtypes = [vp]
+        L.cf_plan_arena_bytes.restype = ctypes.c_size_t
+        L.cf_plan_run.argtypes = [vp, vp, vp, ctypes.c_float, vp, vp]
+        L.cf_plan_status.argtypes = [vp]
+        L.cf_plan_set_timing.argtypes = [vp, ctypes.c_int]
+        L.cf_plan_phase_ms.argtypes = [vp, f32p, ctypes.c_int32]
+        L.cf_plan_launches.argtypes = [vp]
+        L.cf_plan_group.argtypes = [vp]
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-                     "cf_engine_set_mode", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe"):
+                     "cf_engine_set_mode", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
+                     "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
+                     "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group"):
             getattr(L, name).restype = ctypes.c_int
-        if hasattr(L, "cf_sample"):
-            L.cf_sample.restype = ctypes.c_int
         _lib = L
         return L
 
@@ -212,6 +224,61 @@ class Engine:
             base = int(B.offsets[b]) * n_samples
             res.append([raw[base + t * L: base + (t + 1) * L] for t in range(n_samples)])
         return res
+
+
+class Plan:
+    """A device-resident batch (cf_plan_*): fixed lengths, resident descriptors
+    and arena; `run` launches kernels only, on the given CUDA stream."""
+
+    def __init__(self, engine: "Engine", job: int, offsets: np.ndarray):
+        self.engine = engine
+        self.lib = engine.lib
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.n = len(self.offsets) - 1
+        self._h = ctypes.c_void_p()
+        engine._check(self.lib.cf_plan_create(engine._h, int(job), _p(self.offsets, ctypes.c_int64),
+                                              ctypes.c_int32(self.n), ctypes.byref(self._h)))
+
+    @property
+    def arena_bytes(self) -> int:
+        return int(self.lib.cf_plan_arena_bytes(self._h))
+
+    @property
+    def group(self) -> int:
+        return int(self.lib.cf_plan_group(self._h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.cf_plan_launches(self._h))
+
+    def run(self, d_seqs: int, d_mask: int, d_out: int, gamma: float = 6.0, stream: int = 0):
+        """Device pointers (ints) in, asynchronous on `stream` (a cudaStream_t handle)."""
+        self.engine._check(self.lib.cf_plan_run(self._h, ctypes.c_void_p(d_seqs or None),
+                                                ctypes.c_void_p(d_mask or None),
+                                                ctypes.c_float(float(np.float32(gamma))),
+                                                ctypes.c_void_p(d_out), ctypes.c_void_p(stream or None)))
+
+    def status(self):
+        self.engine._check(self.lib.cf_plan_status(self._h))
+
+    def set_timing(self, on: bool):
+        self.engine._check(self.lib.cf_plan_set_timing(self._h, 1 if on else 0))
+
+    def phase_ms(self) -> np.ndarray:
+        ms = np.zeros(4, np.float32)
+        self.engine._check(self.lib.cf_plan_phase_ms(self._h, _p(ms, ctypes.c_float), 4))
+        return ms
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.cf_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _engines = {}

@@ -130,6 +130,37 @@ int cf_sample(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
               const uint8_t* mask, int32_t n, int32_t n_samples, uint64_t seed,
               char* out);
 
+/* ---- plans: device-resident batches ----
+ * A plan fixes a batch's shape (lengths from host `offsets`), orders and
+ * groups its sequences, and owns the device descriptors and a work arena sized
+ * for it.  cf_plan_run then only launches kernels: `d_seqs`, `d_mask` (NULL =
+ * no constraint) and `d_out` are device pointers laid out like the host
+ * buffers of the calls above, and the launches are asynchronous on `stream`
+ * (a cudaStream_t; NULL selects the engine's stream).  `d_out` is float[n]
+ * for CF_JOB_LOGZ, double[n] for CF_JOB_LOGZ64 and the dot-bracket buffer
+ * for CF_JOB_MEA / CF_JOB_MFE.  No reference counterpart: the reference
+ * re-uploads everything per call (gpu.py:500-514). */
+#define CF_JOB_LOGZ   0
+#define CF_JOB_LOGZ64 1
+#define CF_JOB_MEA    3
+#define CF_JOB_MFE    4
+typedef struct cf_plan cf_plan;
+int cf_plan_create(cf_engine* eng, int32_t job, const int64_t* offsets, int32_t n,
+                   cf_plan** out);
+int cf_plan_destroy(cf_plan* plan);
+size_t cf_plan_arena_bytes(const cf_plan* plan);
+int cf_plan_run(cf_plan* plan, const uint8_t* d_seqs, const uint8_t* d_mask, float gamma,
+                void* d_out, void* stream);
+/* Synchronises the device and returns the device-side status of past runs. */
+int cf_plan_status(cf_plan* plan);
+/* Per-phase CUDA-event timing of each run (0 inside, 1 outside, 2 posterior,
+ * 3 decode); cf_plan_phase_ms waits for the last run and returns milliseconds. */
+int cf_plan_set_timing(cf_plan* plan, int on);
+int cf_plan_phase_ms(cf_plan* plan, float* ms, int32_t nphases);
+/* Kernels launched by the last cf_plan_run; sequences per CTA of the plan. */
+int cf_plan_launches(const cf_plan* plan);
+int cf_plan_group(const cf_plan* plan);
+
 #ifdef __cplusplus
 }
 #endif

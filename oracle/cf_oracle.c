@@ -390,6 +390,15 @@ void oracle_viterbi64(const int8_t* s, int L, const int8_t* forced, const double
 
 /* =========================== FP32 =========================== */
 
+/* Optional per-thread counters of guarded semiring updates (the roofline's
+ * algorithmic unit), by category:
+ *   0 inside single-branch LSE   1 inside bifurcation LSE   2 inside other terms
+ *   3 outside single-branch LSE  4 outside bifurcation LSE  5 outside other terms
+ *   6 posterior fexp terms       7 MEA max-plus candidates                     */
+#define CF_NCOUNT 8
+static __thread int64_t* g_cnt = NULL;
+#define CNT(k) do { if (g_cnt) g_cnt[k]++; } while (0)
+
 static inline float lse32(float a, float b) {
     if (a < b) { float t = a; a = b; b = t; }
     if (b < HALF32) return a;
@@ -486,11 +495,11 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
             float FM2 = NEG32;
             for (int k = i + 1; k < j; ++k)
                 if (T(FM1, i, k) > HALF32 && T(FM, k, j) > HALF32)
-                    FM2 = lse32(FM2, T(FM1, i, k) + T(FM, k, j));
+                    { CNT(1); FM2 = lse32(FM2, T(FM1, i, k) + T(FM, k, j)); }
             if (0 < i && j < L && OK_PAIR(i, j + 1)) {
                 float sum = NEG32;
                 float jB = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                sum = lse32(sum, jB + P.hp[j - i <= DHP ? j - i : DHP]);
+                CNT(2); sum = lse32(sum, jB + P.hp[j - i <= DHP ? j - i : DHP]);
                 int pmax = i + CMAX < j ? i + CMAX : j;
                 for (int p = i; p <= pmax; ++p) {
                     int l1 = p - i;
@@ -511,7 +520,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                                 else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
                                 e = P.cs[l1 * 31 + l2] + P.bp[I2(s[p + 1], s[q])] + jB1 + jB2 + snuc;
                             }
-                            sum = lse32(sum, e + T(FC, p + 1, q - 1));
+                            CNT(0); sum = lse32(sum, e + T(FC, p + 1, q - 1));
                         }
                     }
                 }
@@ -519,7 +528,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                     float jA = P.hc[I2(s[i], s[j + 1])];
                     if (i < L) jA += P.dl[I3(s[i], s[j + 1], s[i + 1])];
                     if (j > 0) jA += P.dr[I3(s[i], s[j + 1], s[j])];
-                    sum = lse32(sum, FM2 + jA + P.mp + P.mb);
+                    CNT(2); sum = lse32(sum, FM2 + jA + P.mp + P.mb);
                 }
                 T(FC, i, j) = sum;
             }
@@ -529,16 +538,16 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                     float jAji = P.hc[I2(s[j], s[i + 1])];
                     if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
                     if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    sum = lse32(sum, T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
+                    CNT(2); sum = lse32(sum, T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
                 }
-                if (T(FM1, i + 1, j) > HALF32) sum = lse32(sum, T(FM1, i + 1, j) + P.mu);
+                if (T(FM1, i + 1, j) > HALF32) { CNT(2); sum = lse32(sum, T(FM1, i + 1, j) + P.mu); }
                 T(FM1, i, j) = sum;
             }
             if (0 < i && i + 2 <= j && j < L) {
                 float sum = NEG32;
-                if (FM2 > HALF32) sum = lse32(sum, FM2);
-                if (T(FM, i, j - 1) > HALF32) sum = lse32(sum, T(FM, i, j - 1) + P.mu);
-                if (T(FM1, i, j) > HALF32) sum = lse32(sum, T(FM1, i, j));
+                if (FM2 > HALF32) { CNT(2); sum = lse32(sum, FM2); }
+                if (T(FM, i, j - 1) > HALF32) { CNT(2); sum = lse32(sum, T(FM, i, j - 1) + P.mu); }
+                if (T(FM1, i, j) > HALF32) { CNT(2); sum = lse32(sum, T(FM1, i, j)); }
                 T(FM, i, j) = sum;
             }
         }
@@ -551,7 +560,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                 float jA = P.hc[I2(s[j], s[k + 1])];
                 if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
                 if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
-                sum = lse32(sum, F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
+                CNT(2); sum = lse32(sum, F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
             }
         }
         F5[j] = sum;
@@ -561,15 +570,15 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
     /* ---------- outside (cpu.py:680-758) ---------- */
     F5o[L] = ZERO;
     for (int j = L; j > 0; --j) {
-        F5o[j - 1] = lse32(F5o[j - 1], F5o[j] + P.eu);
+        CNT(5); F5o[j - 1] = lse32(F5o[j - 1], F5o[j] + P.eu);
         for (int k = 0; k < j; ++k) {
             if (OK_PAIR(k + 1, j)) {
                 float jA = P.hc[I2(s[j], s[k + 1])];
                 if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
                 if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
                 float temp = F5o[j] + P.ep + P.bp[I2(s[k + 1], s[j])] + jA;
-                if (T(FC, k + 1, j - 1) > HALF32) F5o[k] = lse32(F5o[k], temp + T(FC, k + 1, j - 1));
-                if (F5[k] > HALF32) T(FCo, k + 1, j - 1) = lse32(T(FCo, k + 1, j - 1), temp + F5[k]);
+                if (T(FC, k + 1, j - 1) > HALF32) { CNT(5); F5o[k] = lse32(F5o[k], temp + T(FC, k + 1, j - 1)); }
+                if (F5[k] > HALF32) { CNT(5); T(FCo, k + 1, j - 1) = lse32(T(FCo, k + 1, j - 1), temp + F5[k]); }
             }
         }
     }
@@ -577,7 +586,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
         for (int j = L; j >= i; --j) {
             float FM2o = NEG32;
             if (0 < i && i + 2 <= j && j < L) {
-                FM2o = lse32(FM2o, T(FMo, i, j));
+                CNT(5); CNT(5); CNT(5); FM2o = lse32(FM2o, T(FMo, i, j));
                 T(FMo, i, j - 1) = lse32(T(FMo, i, j - 1), T(FMo, i, j) + P.mu);
                 T(FM1o, i, j) = lse32(T(FM1o, i, j), T(FMo, i, j));
             }
@@ -586,9 +595,9 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                     float jAji = P.hc[I2(s[j], s[i + 1])];
                     if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
                     if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    T(FCo, i + 1, j - 1) = lse32(T(FCo, i + 1, j - 1), T(FM1o, i, j) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
+                    CNT(5); T(FCo, i + 1, j - 1) = lse32(T(FCo, i + 1, j - 1), T(FM1o, i, j) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
                 }
-                T(FM1o, i + 1, j) = lse32(T(FM1o, i + 1, j), T(FM1o, i, j) + P.mu);
+                CNT(5); T(FM1o, i + 1, j) = lse32(T(FM1o, i + 1, j), T(FM1o, i, j) + P.mu);
             }
             if (0 < i && j < L && OK_PAIR(i, j + 1)) {
                 float fco = T(FCo, i, j);
@@ -613,20 +622,20 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                                     else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
                                     e = P.cs[l1 * 31 + l2] + P.bp[I2(s[p + 1], s[q])] + jB_ij + jB2 + snuc;
                                 }
-                                T(FCo, p + 1, q - 1) = lse32(T(FCo, p + 1, q - 1), fco + e);
+                                CNT(3); T(FCo, p + 1, q - 1) = lse32(T(FCo, p + 1, q - 1), fco + e);
                             }
                         }
                     }
                     float jA = P.hc[I2(s[i], s[j + 1])];
                     if (i < L) jA += P.dl[I3(s[i], s[j + 1], s[i + 1])];
                     if (j > 0) jA += P.dr[I3(s[i], s[j + 1], s[j])];
-                    FM2o = lse32(FM2o, fco + jA + P.mp + P.mb);
+                    CNT(5); FM2o = lse32(FM2o, fco + jA + P.mp + P.mb);
                 }
             }
             if (FM2o > HALF32) {
                 for (int k = i + 1; k < j; ++k) {
-                    if (T(FM, k, j) > HALF32) T(FM1o, i, k) = lse32(T(FM1o, i, k), FM2o + T(FM, k, j));
-                    if (T(FM1, i, k) > HALF32) T(FMo, k, j) = lse32(T(FMo, k, j), FM2o + T(FM1, i, k));
+                    if (T(FM, k, j) > HALF32) { CNT(4); T(FM1o, i, k) = lse32(T(FM1o, i, k), FM2o + T(FM, k, j)); }
+                    if (T(FM1, i, k) > HALF32) { CNT(4); T(FMo, k, j) = lse32(T(FMo, k, j), FM2o + T(FM1, i, k)); }
                 }
             }
         }
@@ -659,7 +668,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                                     else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
                                     e = outside + jB_ij + P.cs[l1 * 31 + l2] + T(FC, p + 1, q - 1) + P.bp[I2(s[p + 1], s[q])] + jB2 + snuc;
                                 }
-                                T(POST, p + 1, q) += fexp32(e);
+                                CNT(6); T(POST, p + 1, q) += fexp32(e);
                             }
                         }
                     }
@@ -670,7 +679,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                     float jAji = P.hc[I2(s[j], s[i + 1])];
                     if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
                     if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    T(POST, i + 1, j) += fexp32(T(FM1o, i, j) + T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])] - Z);
+                    CNT(6); T(POST, i + 1, j) += fexp32(T(FM1o, i, j) + T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])] - Z);
                 }
             }
         }
@@ -683,7 +692,7 @@ float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const flo
                     float jA = P.hc[I2(s[j], s[k + 1])];
                     if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
                     if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
-                    T(POST, k + 1, j) += fexp32(outside + F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
+                    CNT(6); T(POST, k + 1, j) += fexp32(outside + F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
                 }
             }
         }
@@ -728,17 +737,17 @@ void oracle_mea_decode32(const float* POST, int L, const int8_t* forced, const i
             if (i == j) {
                 if (F(0.0) > S(i, j)) { S(i, j) = F(0.0); TB(i, j) = 0; }
             } else {
-                float v = up[i + 1] + S(i + 1, j);
+                CNT(7); CNT(7); float v = up[i + 1] + S(i + 1, j);
                 if (v > S(i, j)) { S(i, j) = v; TB(i, j) = 1; }
                 v = up[j] + S(i, j - 1);
                 if (v > S(i, j)) { S(i, j) = v; TB(i, j) = 2; }
                 if (i + 2 <= j) {
                     if (OK_PAIR(i + 1, j)) {
-                        v = T(POST, i + 1, j) + S(i + 1, j - 1);
+                        CNT(7); v = T(POST, i + 1, j) + S(i + 1, j - 1);
                         if (v > S(i, j)) { S(i, j) = v; TB(i, j) = 3; }
                     }
                     for (int k = i + 1; k < j; ++k) {
-                        v = S(i, k) + S(k, j);
+                        CNT(7); v = S(i, k) + S(k, j);
                         if (v > S(i, j)) { S(i, j) = v; TB(i, j) = k + 4; }
                     }
                 }
@@ -859,4 +868,19 @@ int oracle_batch(int job, const uint8_t* seqs, const int64_t* offs, const uint8_
     free(th);
     pthread_mutex_destroy(&B.mu);
     return 0;
+}
+
+/* Count the guarded updates of one MEA fold (posterior + decode) into cnt[8]. */
+void oracle_count_mea_ops(const int8_t* s, int L, const int8_t* forced, const float* blob, float gamma,
+                          int64_t* cnt) {
+    const int n = L + 2;
+    float* POST = (float*)malloc(sizeof(float) * (size_t)n * n);
+    int64_t* pair = (int64_t*)malloc(sizeof(int64_t) * n);
+    for (int k = 0; k < CF_NCOUNT; ++k) cnt[k] = 0;
+    g_cnt = cnt;
+    oracle_posterior32(s, L, forced, blob, POST, NULL);
+    oracle_mea_decode32(POST, L, forced, s, gamma, pair);
+    g_cnt = NULL;
+    free(pair);
+    free(POST);
 }

@@ -55,6 +55,8 @@ def lib():
         L.oracle_lse32.argtypes = [ctypes.c_float, ctypes.c_float]
         L.oracle_fexp32.restype = ctypes.c_float
         L.oracle_fexp32.argtypes = [ctypes.c_float]
+        L.oracle_count_mea_ops.restype = None
+        L.oracle_count_mea_ops.argtypes = [i8p, ctypes.c_int, i8p, f32p, ctypes.c_float, i64p]
         u8p = P(ctypes.c_uint8)
         L.oracle_batch.restype = ctypes.c_int
         L.oracle_batch.argtypes = [ctypes.c_int, u8p, i64p, u8p, ctypes.c_int, f32p, f64p,
@@ -198,3 +200,23 @@ def batch(job, seqs, P, masks=None, gamma=6.0, threads=None):
         raw = out_s.raw[:int(offs[-1])].decode("ascii")
         return [raw[offs[b]:offs[b + 1]] for b in range(n)]
     return [float(z) for z in out_z[:n]]
+
+
+# Cost, in FP32 operations, of one guarded update of each counter category
+# (oracle_count_mea_ops): single-branch LSE = 5 adds for the loop score +
+# 1 add of the inner value + 8 for Fast_LogPlusEquals; bifurcation / other
+# LSE = 1 add + 8; posterior term = 7 adds + 8 (Fast_Exp) + 1 accumulate;
+# MEA candidate = 1 add (the compare is not counted).
+OP_COST = (14, 9, 9, 14, 9, 9, 16, 1)
+COUNT_NAMES = ("inside_single", "inside_bif", "inside_other", "outside_single", "outside_bif",
+               "outside_other", "posterior_terms", "mea_candidates")
+
+
+def count_mea_ops(seq, P, forced=None, gamma=6.0):
+    """Guarded-update counts of one MEA fold, per category (COUNT_NAMES)."""
+    s, fo, L = encode(seq, forced)
+    b32, _ = _blobs(P)
+    cnt = np.zeros(8, np.int64)
+    lib().oracle_count_mea_ops(_ptr(s, ctypes.c_int8), L, _ptr(fo, ctypes.c_int8), _ptr(b32, ctypes.c_float),
+                               float(np.float32(gamma)), _ptr(cnt, ctypes.c_int64))
+    return cnt

@@ -13,7 +13,7 @@ HEADER = os.path.join(REPO, "include", "contrafold_gb300.h")
 
 def header_symbols():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*|void)\s+(cf_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*|void)\s+(cf_\w+)\s*\(", txt, re.M)))
 
 
 def test_header_layout_matches_python(P):
