@@ -236,7 +236,9 @@ def our_arm(args):
     d_mask = torch.from_numpy(mask.reshape(-1).copy()).to(dev)
     d_out = torch.empty(n * L, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: its handle is what the plan launches on and what the
+    # CUDA events below are recorded on (the legacy default stream's handle is 0)
+    stream = torch.cuda.Stream(dev)
 
     def sync_all():
         torch.cuda.synchronize(dev)
@@ -252,7 +254,8 @@ def our_arm(args):
         plan.status()
         step_ms, phase = [], np.zeros(4)
         for _ in range(args.steps):
-            flush.fill_(1)
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
             sync_all()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
