@@ -45,37 +45,49 @@ __host__ __device__ __forceinline__ int tri_off(int d, int m) { return d * m - (
 // Round a word count up to 32 words (128 bytes).
 __host__ __device__ __forceinline__ int64_t pad32(int64_t w) { return (w + 31) & ~int64_t(31); }
 
-// FP32 fold arena of one sequence (words).  The inside tables come first so
-// an inside-only arena (logZ, sampling) is a prefix of the full one.
-// Aliases: POST reuses FMo after the outside pass; the MEA score table reuses
-// FM2o and its argmax table FM.
+// Pairable-cell list of one sequence (see cf_seq.cuh): poff[L+2] int32 and
+// pl[tri_size(L)] int16, in 4-byte words.
+__host__ __device__ __forceinline__ int64_t plist_words(int L) {
+    return pad32(L + 3) + pad32(tri_size(L) / 2 + 1);
+}
+
+// FP32 fold arena of one sequence (words).  The inside tables and the pair
+// list come first so an inside-only arena (logZ, sampling) is a prefix of the
+// full one.  Aliases: POST reuses FMo after the outside pass; the MEA score
+// table reuses FM2o and its argmax table FM.
 struct Arena32 {
-    int64_t FC, FM, FM1, F5, FCo, FMo, FM1o, FM2o, F5o, up, queue, total;
+    int64_t FC, FM, FM1, F5, FB, PL, FCo, FMo, FM1o, FM2o, F5o, up, queue, total;
 };
 __host__ __device__ __forceinline__ Arena32 arena32(int L) {
     Arena32 a;
     const int64_t t = pad32(tri_size(L));
     const int64_t v = pad32(L + 2);
-    a.FC = 0; a.FM = t; a.FM1 = 2 * t; a.F5 = 3 * t;
-    a.FCo = 3 * t + v; a.FMo = 4 * t + v; a.FM1o = 5 * t + v; a.FM2o = 6 * t + v;
-    a.F5o = 7 * t + v; a.up = a.F5o + v; a.queue = a.up + v;
+    a.FC = 0; a.FM = t; a.FM1 = 2 * t; a.F5 = 3 * t; a.FB = 3 * t + v; a.PL = a.FB + 2 * v;
+    const int64_t o = a.PL + plist_words(L);
+    a.FCo = o; a.FMo = o + t; a.FM1o = o + 2 * t; a.FM2o = o + 3 * t;
+    a.F5o = o + 4 * t; a.up = a.F5o + v; a.queue = a.up + v;
     a.total = a.queue + pad32(4 * (int64_t)L + 16);
     return a;
 }
-// Inside-only arena (logZ, sampling): FC FM FM1 F5, the prefix of Arena32.
+// Inside-only arena (logZ, sampling): FC FM FM1 F5, the FM2 step buffers and
+// the pair list -- the prefix of Arena32.
 __host__ __device__ __forceinline__ int64_t arena32_inside_words(int L) {
-    return 3 * pad32(tri_size(L)) + pad32(L + 2);
+    return 3 * pad32(tri_size(L)) + 3 * pad32(L + 2) + plist_words(L);
 }
-// FP64 arena (Viterbi / exact logZ), in 4-byte words: FC FM FM1 (doubles), F5, stack.
+// FP64 arena (Viterbi / exact logZ): FC FM FM1 F5 in doubles, then (in 4-byte
+// words) the pair list and the traceback stack.
 struct Arena64 {
-    int64_t FC, FM, FM1, F5, stack, total;   // offsets in doubles except stack (ints, after)
+    int64_t FC, FM, FM1, F5, FB;   // offsets in doubles (FB: two FM2 step buffers)
+    int64_t PL, stack, total;      // offsets in 4-byte words
 };
 __host__ __device__ __forceinline__ Arena64 arena64(int L) {
     Arena64 a;
     const int64_t t = pad32(tri_size(L));
-    a.FC = 0; a.FM = t; a.FM1 = 2 * t; a.F5 = 3 * t; a.stack = 3 * t + pad32(L + 2);
-    // total in 4-byte words: doubles * 2 + 3 int stacks of 4L+16
-    a.total = a.stack * 2 + pad32(3 * (4 * (int64_t)L + 16));
+    const int64_t v = pad32(L + 2);
+    a.FC = 0; a.FM = t; a.FM1 = 2 * t; a.F5 = 3 * t; a.FB = 3 * t + v;
+    a.PL = 2 * (3 * t + 3 * v);
+    a.stack = a.PL + plist_words(L);
+    a.total = a.stack + pad32(3 * (4 * (int64_t)L + 16));
     return a;
 }
 

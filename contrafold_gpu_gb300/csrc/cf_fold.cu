@@ -13,7 +13,8 @@
 namespace cf {
 
 // ---------------------------------------------------------------------------
-// Shared-memory carve-up
+// Shared memory: parameter tables + group descriptors, then per sequence the
+// codes (s, pc) and the four partner bit sets.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct SmemFold {
@@ -24,18 +25,30 @@ struct SmemFold {
     int64_t soff[kMaxGroup];
     int idx[kMaxGroup];
     int n;        // sequences in this group
+    int gcap;     // sequences per CTA of the launch (sizes the dynamic region)
     int Lmax;
 };
 
+__host__ __device__ __forceinline__ int code_stride(int Lmax) { return (Lmax + 2 + 15) & ~15; }
+
 template <typename R>
-__device__ __forceinline__ int8_t* seq_smem(SmemFold<R>* sm) {
-    return reinterpret_cast<int8_t*>(sm + 1);
+__device__ __forceinline__ unsigned char* dyn_smem(SmemFold<R>* sm) {
+    return reinterpret_cast<unsigned char*>(sm + 1);
 }
 
-// Load tables + group descriptors + encoded sequences.  Returns stride of
-// the per-sequence code arrays.
 template <typename R>
-__device__ __forceinline__ int setup_group(SmemFold<R>* sm, const FoldArgs& A, const R* __restrict__ gblob) {
+__device__ __forceinline__ SeqV seq_v(SmemFold<R>* sm, int g) {
+    const int cs = code_stride(sm->Lmax), W = pb_words(sm->Lmax);
+    unsigned char* base = dyn_smem(sm);
+    const int8_t* s = reinterpret_cast<const int8_t*>(base + (2 * g) * cs);
+    const int8_t* pc = reinterpret_cast<const int8_t*>(base + (2 * g + 1) * cs);
+    const uint32_t* PB = reinterpret_cast<const uint32_t*>(base + 2 * sm->gcap * cs) + (size_t)g * 4 * W;
+    return SeqV{s, pc, PB, W, sm->L[g]};
+}
+
+// Load tables, group descriptors, sequence codes and partner bit sets.
+template <typename R>
+__device__ __forceinline__ void setup_group(SmemFold<R>* sm, const FoldArgs& A, const R* __restrict__ gblob) {
     const int g0 = blockIdx.x * A.group;
     const int ng = min(A.group, A.n - g0);
     if (threadIdx.x == 0) {
@@ -49,32 +62,271 @@ __device__ __forceinline__ int setup_group(SmemFold<R>* sm, const FoldArgs& A, c
             lmax = max(lmax, D.L);
         }
         sm->n = ng;
+        sm->gcap = A.group;
         sm->Lmax = lmax;
     }
     load_tabs(&sm->tabs, gblob);
     load_poly_tables(&sm->poly);
     __syncthreads();
-    const int stride = (sm->Lmax + 2 + 15) & ~15;
-    int8_t* base = seq_smem(sm);
-    for (int g = 0; g < sm->n; ++g)
-        encode_seq(A.seqs, A.mask, sm->soff[g], sm->L[g], base + (2 * g) * stride, base + (2 * g + 1) * stride);
+    const int cs = code_stride(sm->Lmax), W = pb_words(sm->Lmax);
+    unsigned char* base = dyn_smem(sm);
+    for (int g = 0; g < sm->n; ++g) {
+        int8_t* s = reinterpret_cast<int8_t*>(base + (2 * g) * cs);
+        int8_t* pc = reinterpret_cast<int8_t*>(base + (2 * g + 1) * cs);
+        uint32_t* PB = reinterpret_cast<uint32_t*>(base + 2 * sm->gcap * cs) + (size_t)g * 4 * W;
+        build_seq(A.seqs, A.mask, sm->soff[g], sm->L[g], W, s, pc, PB);
+    }
     __syncthreads();
-    return stride;
 }
+
+// ---------------------------------------------------------------------------
+// Arena views
+// ---------------------------------------------------------------------------
+template <typename R>
+struct InView {
+    InTabs<R> T;
+    R* FB;        // two FM2 step buffers of stride fbs
+    int fbs;
+    PairList PLs;
+};
 
 template <typename R>
-__device__ __forceinline__ SeqView seq_view(SmemFold<R>* sm, int stride, int g) {
-    int8_t* base = seq_smem(sm);
-    return SeqView{base + (2 * g) * stride, base + (2 * g + 1) * stride, sm->L[g]};
+__device__ __forceinline__ InView<R> in_view(const FoldArgs& A, int64_t ws_off, int L) {
+    InView<R> V;
+    if (sizeof(R) == 4) {
+        const Arena32 a = arena32(L);
+        float* base = A.ws + ws_off;
+        V.T.FC = reinterpret_cast<R*>(base + a.FC);
+        V.T.FM = reinterpret_cast<R*>(base + a.FM);
+        V.T.FM1 = reinterpret_cast<R*>(base + a.FM1);
+        V.T.F5 = reinterpret_cast<R*>(base + a.F5);
+        V.FB = reinterpret_cast<R*>(base + a.FB);
+        V.PLs = plist_at(base + a.PL, L);
+    } else {
+        const Arena64 a = arena64(L);
+        double* base = reinterpret_cast<double*>(A.ws + ws_off);
+        V.T.FC = reinterpret_cast<R*>(base + a.FC);
+        V.T.FM = reinterpret_cast<R*>(base + a.FM);
+        V.T.FM1 = reinterpret_cast<R*>(base + a.FM1);
+        V.T.F5 = reinterpret_cast<R*>(base + a.F5);
+        V.FB = reinterpret_cast<R*>(base + a.FB);
+        V.PLs = plist_at(A.ws + ws_off + a.PL, L);
+    }
+    V.T.m = L + 1;
+    V.fbs = (int)pad32(L + 2);
+    return V;
 }
 
-// Walk diagonals d = d_begin .. d_end (step +1 or -1) over all sequences of
-// the group; call f(g, i, i + d) for every cell.
+__device__ __forceinline__ OutTabs out_tabs(const FoldArgs& A, int64_t ws_off, int L) {
+    const Arena32 a = arena32(L);
+    float* base = A.ws + ws_off;
+    OutTabs T;
+    T.FC = base + a.FC; T.FM = base + a.FM; T.FM1 = base + a.FM1; T.F5 = base + a.F5;
+    T.FCo = base + a.FCo; T.FMo = base + a.FMo; T.FM1o = base + a.FM1o; T.FM2o = base + a.FM2o;
+    T.F5o = base + a.F5o;
+    T.m = L + 1;
+    return T;
+}
+
+__device__ __forceinline__ PairList plist_of(const FoldArgs& A, int64_t ws_off, int L) {
+    return plist_at(A.ws + ws_off + arena32(L).PL, L);
+}
+
+// ---------------------------------------------------------------------------
+// One pipelined step over the group: phase-B items (pairable cells of
+// diagonal dB, from the pair lists) then phase-A items (every cell of
+// diagonal dA).  The B block is padded to a multiple of 32 so that each warp
+// holds one kind of item.  fB(g, i), fA(g, i) process one cell.
+// ---------------------------------------------------------------------------
+template <typename R, typename GetPL, typename FB, typename FA>
+__device__ __forceinline__ void step_items(SmemFold<R>* sm, int dB, int dA, GetPL getpl, FB fB, FA fA) {
+    const int ng = sm->n;
+    int NB = 0, NA = 0;
+    for (int g = 0; g < ng; ++g) {
+        const int L = sm->L[g];
+        if (dB >= 0 && dB <= L - 2) {
+            const PairList PLs = getpl(g);
+            NB += PLs.poff[dB + 1] - PLs.poff[dB];
+        }
+        if (dA >= 0) NA += max(0, L + 1 - dA);
+    }
+    const int NB32 = (NB + 31) & ~31;
+    for (int c = threadIdx.x; c < NB32 + NA; c += blockDim.x) {
+        if (c < NB32) {
+            if (c >= NB) continue;
+            int r = c, g = 0;
+            for (;; ++g) {
+                const int L = sm->L[g];
+                if (dB <= L - 2) {
+                    const PairList PLs = getpl(g);
+                    const int o = PLs.poff[dB], cnt = PLs.poff[dB + 1] - o;
+                    if (r < cnt) { fB(g, (int)PLs.pl[o + r]); break; }
+                    r -= cnt;
+                }
+            }
+        } else {
+            int r = c - NB32, g = 0;
+            for (;; ++g) {
+                const int cnt = max(0, sm->L[g] + 1 - dA);
+                if (r < cnt) { fA(g, r); break; }
+                r -= cnt;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Inside (any semiring): pair lists, FC/FM/FM1 wavefront, F5.
+// ---------------------------------------------------------------------------
+template <class S>
+__device__ __forceinline__ S make_sr(const PolyTables* pt);
+template <>
+__device__ __forceinline__ Lse32 make_sr<Lse32>(const PolyTables* pt) { return Lse32{pt}; }
+template <>
+__device__ __forceinline__ LseAcc32 make_sr<LseAcc32>(const PolyTables*) { return LseAcc32{}; }
+template <>
+__device__ __forceinline__ Lse64 make_sr<Lse64>(const PolyTables*) { return Lse64{}; }
+template <>
+__device__ __forceinline__ Max64 make_sr<Max64>(const PolyTables*) { return Max64{}; }
+
+template <class S>
+__device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, const FoldArgs& A) {
+    using R = typename S::Real;
+    const S sr = make_sr<S>(&sm->poly);
+    for (int g = 0; g < sm->n; ++g) build_plist(seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).PLs);
+    auto getpl = [&](int g) { return in_view<R>(A, sm->ws[g], sm->L[g]).PLs; };
+    for (int t = 0; t <= sm->Lmax + 1; ++t) {
+        step_items(
+            sm, t - 1, t <= sm->Lmax ? t : -1, getpl,
+            [&](int g, int i) {   // phase B(t-1): FC of a pairable cell
+                const SeqV Q = seq_v(sm, g);
+                const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
+                const R fm2 = V.FB[((t - 1) & 1) * V.fbs + i];
+                inside_B<S>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2);
+            },
+            [&](int g, int i) {   // phase A(t): FM2, FM1, FM
+                const SeqV Q = seq_v(sm, g);
+                const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
+                V.FB[(t & 1) * V.fbs + i] = inside_A<S>(sr, &sm->tabs, Q, V.T, i, i + t);
+            });
+    }
+    // exterior recurrence: one warp per sequence
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int g = warp; g < sm->n; g += nwarps)
+        exterior_warp<S>(sr, &sm->tabs, seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).T);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kFoldThreads) k_inside32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    inside_group<Lse32>(sm, A);
+    if (A.logz != nullptr)
+        for (int g = threadIdx.x; g < sm->n; g += blockDim.x)
+            A.logz[sm->idx[g]] = in_view<float>(A, sm->ws[g], sm->L[g]).T.F5[sm->L[g]];
+}
+
+// Same recurrence with accurate float32 log-sum-exp: logZ_batch and the sampler.
+__global__ void __launch_bounds__(kFoldThreads) k_inside32acc(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    inside_group<LseAcc32>(sm, A);
+    if (A.logz != nullptr)
+        for (int g = threadIdx.x; g < sm->n; g += blockDim.x)
+            A.logz[sm->idx[g]] = in_view<float>(A, sm->ws[g], sm->L[g]).T.F5[sm->L[g]];
+}
+
+__global__ void __launch_bounds__(kFoldThreads) k_inside64(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<double>*>(smem_raw);
+    setup_group(sm, A, A.blob64);
+    inside_group<Lse64>(sm, A);
+    for (int g = threadIdx.x; g < sm->n; g += blockDim.x)
+        A.logz64[sm->idx[g]] = in_view<double>(A, sm->ws[g], sm->L[g]).T.F5[sm->L[g]];
+}
+
+// ---------------------------------------------------------------------------
+// Outside + posterior + MEA (FP32)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    const Lse32 sr{&sm->poly};
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int g = warp; g < sm->n; g += nwarps)
+        exterior_outside_warp(sr, &sm->tabs, seq_v(sm, g), out_tabs(A, sm->ws[g], sm->L[g]));
+    __syncthreads();
+    auto getpl = [&](int g) { return plist_of(A, sm->ws[g], sm->L[g]); };
+    for (int t = sm->Lmax; t >= 0; --t) {
+        step_items(
+            sm, t - 1, t, getpl,
+            [&](int g, int a) {   // phase B(t-1): FCo of a pairable cell
+                const SeqV Q = seq_v(sm, g);
+                outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1);
+            },
+            [&](int g, int a) {   // phase A(t): FMo, FM1o, FM2o
+                const SeqV Q = seq_v(sm, g);
+                outside_A(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t);
+            });
+    }
+}
+
+// Posterior of every pairable pair; POST goes to the FMo slot (triangular,
+// zero elsewhere) and, for cf_bpp, densely into the caller's L x L matrix.
+__global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    for (int g = 0; g < sm->n; ++g) {
+        const int L = sm->L[g];
+        float* POST = out_tabs(A, sm->ws[g], L).FMo;
+        const int64_t tot = tri_size(L);
+        for (int64_t c = threadIdx.x; c < tot; c += blockDim.x) POST[c] = 0.0f;
+        if (A.post_out) {
+            float* dense = A.post_out + A.post_offs[sm->idx[g]];
+            for (int64_t c = threadIdx.x; c < (int64_t)L * L; c += blockDim.x) dense[c] = 0.0f;
+        }
+    }
+    __syncthreads();
+    for (int g = 0; g < sm->n; ++g) {
+        const SeqV Q = seq_v(sm, g);
+        const int L = Q.L, m = L + 1;
+        const OutTabs T = out_tabs(A, sm->ws[g], L);
+        const PairList PLs = plist_of(A, sm->ws[g], L);
+        const float Z = T.F5[L];
+        float* POST = T.FMo;
+        float* dense = A.post_out ? A.post_out + A.post_offs[sm->idx[g]] : nullptr;
+        // pairable FC cells (i, i+d) <-> pairs (a, b) = (i, i+d+1), walked in
+        // list order (thread k takes entries k, k + blockDim, ...)
+        int c = threadIdx.x;
+        for (int d = 0; d <= L - 2; ++d) {
+            const int o = PLs.poff[d], cnt = PLs.poff[d + 1] - o;
+            for (; c < cnt; c += blockDim.x) {
+                const int a = PLs.pl[o + c], b = a + d + 1;
+                const float v = posterior_pair(&sm->tabs, &sm->poly, Q, T, Z, a, b);
+                POST[tri_off(d + 1, m) + a] = v;
+                if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
+            }
+            c -= cnt;
+        }
+    }
+    if (A.logz != nullptr)
+        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
+            const OutTabs T = out_tabs(A, sm->ws[g], sm->L[g]);
+            A.logz[sm->idx[g]] = T.F5[sm->L[g]];
+        }
+}
+
+// Walk diagonals d = d_begin .. d_end (step +1) over all sequences of the
+// group; call f(g, i, i + d) for every cell.  One barrier per diagonal.
 template <typename R, typename F>
 __device__ __forceinline__ void wavefront(SmemFold<R>* sm, int d_begin, int d_end, int step, F f) {
     const int ng = sm->n;
     for (int d = d_begin; step > 0 ? d <= d_end : d >= d_end; d += step) {
-        // cells of sequence g on diagonal d: L_g + 1 - d (if positive)
         int total = 0;
         for (int g = 0; g < ng; ++g) total += max(0, sm->L[g] + 1 - d);
         for (int c = threadIdx.x; c < total; c += blockDim.x) {
@@ -91,173 +343,12 @@ __device__ __forceinline__ void wavefront(SmemFold<R>* sm, int d_begin, int d_en
     }
 }
 
-// ---------------------------------------------------------------------------
-// Inside (any semiring): fills FC/FM/FM1/F5 of each sequence; writes logZ.
-// ---------------------------------------------------------------------------
-template <class S>
-__device__ __forceinline__ InTabs<typename S::Real> in_tabs(const FoldArgs& A, int64_t ws_off, int L) {
-    using R = typename S::Real;
-    InTabs<R> T;
-    if (sizeof(R) == 4) {
-        const Arena32 a = arena32(L);
-        float* base = A.ws + ws_off;
-        T.FC = reinterpret_cast<R*>(base + a.FC);
-        T.FM = reinterpret_cast<R*>(base + a.FM);
-        T.FM1 = reinterpret_cast<R*>(base + a.FM1);
-        T.F5 = reinterpret_cast<R*>(base + a.F5);
-    } else {
-        const Arena64 a = arena64(L);
-        double* base = reinterpret_cast<double*>(A.ws + ws_off);
-        T.FC = reinterpret_cast<R*>(base + a.FC);
-        T.FM = reinterpret_cast<R*>(base + a.FM);
-        T.FM1 = reinterpret_cast<R*>(base + a.FM1);
-        T.F5 = reinterpret_cast<R*>(base + a.F5);
-    }
-    T.m = L + 1;
-    return T;
-}
-
-template <class S>
-__device__ __forceinline__ S make_sr(const PolyTables* pt);
-template <>
-__device__ __forceinline__ Lse32 make_sr<Lse32>(const PolyTables* pt) { return Lse32{pt}; }
-template <>
-__device__ __forceinline__ LseAcc32 make_sr<LseAcc32>(const PolyTables*) { return LseAcc32{}; }
-template <>
-__device__ __forceinline__ Lse64 make_sr<Lse64>(const PolyTables*) { return Lse64{}; }
-template <>
-__device__ __forceinline__ Max64 make_sr<Max64>(const PolyTables*) { return Max64{}; }
-
-template <class S>
-__device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, const FoldArgs& A, int stride) {
-    using R = typename S::Real;
-    const S sr = make_sr<S>(&sm->poly);
-    wavefront(sm, 0, sm->Lmax, +1, [&](int g, int i, int j) {
-        const SeqView Q = seq_view(sm, stride, g);
-        const InTabs<R> T = in_tabs<S>(A, sm->ws[g], Q.L);
-        inside_cell<S>(sr, &sm->tabs, Q, T, i, j);
-    });
-    // exterior recurrence: one warp per sequence
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int g = warp; g < sm->n; g += nwarps) {
-        const SeqView Q = seq_view(sm, stride, g);
-        const InTabs<R> T = in_tabs<S>(A, sm->ws[g], Q.L);
-        exterior_warp<S>(sr, &sm->tabs, Q, T);
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(kFoldThreads) k_inside32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob32);
-    inside_group<Lse32>(sm, A, stride);
-    if (A.logz != nullptr)
-        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-            const InTabs<float> T = in_tabs<Lse32>(A, sm->ws[g], sm->L[g]);
-            A.logz[sm->idx[g]] = T.F5[sm->L[g]];
-        }
-}
-
-// Same recurrence with accurate float32 log-sum-exp: logZ_batch and the sampler.
-__global__ void __launch_bounds__(kFoldThreads) k_inside32acc(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob32);
-    inside_group<LseAcc32>(sm, A, stride);
-    if (A.logz != nullptr)
-        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-            const InTabs<float> T = in_tabs<LseAcc32>(A, sm->ws[g], sm->L[g]);
-            A.logz[sm->idx[g]] = T.F5[sm->L[g]];
-        }
-}
-
-__global__ void __launch_bounds__(kFoldThreads) k_inside64(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<double>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob64);
-    inside_group<Lse64>(sm, A, stride);
-    for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-        const InTabs<double> T = in_tabs<Lse64>(A, sm->ws[g], sm->L[g]);
-        A.logz64[sm->idx[g]] = T.F5[sm->L[g]];
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Outside + posterior + MEA (FP32)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ OutTabs out_tabs(const FoldArgs& A, int64_t ws_off, int L) {
-    const Arena32 a = arena32(L);
-    float* base = A.ws + ws_off;
-    OutTabs T;
-    T.FC = base + a.FC; T.FM = base + a.FM; T.FM1 = base + a.FM1; T.F5 = base + a.F5;
-    T.FCo = base + a.FCo; T.FMo = base + a.FMo; T.FM1o = base + a.FM1o; T.FM2o = base + a.FM2o;
-    T.F5o = base + a.F5o;
-    T.m = L + 1;
-    return T;
-}
-
-__global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob32);
-    const Lse32 sr{&sm->poly};
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int g = warp; g < sm->n; g += nwarps) {
-        const SeqView Q = seq_view(sm, stride, g);
-        exterior_outside_warp(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L));
-    }
-    __syncthreads();
-    wavefront(sm, sm->Lmax, 0, -1, [&](int g, int a, int b) {
-        const SeqView Q = seq_view(sm, stride, g);
-        outside_cell(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, b);
-    });
-}
-
-// Posterior of every pair; POST goes to the FMo slot (triangular) and, for
-// cf_bpp, densely into the caller's L x L matrix.
-__global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob32);
-    for (int g = 0; g < sm->n; ++g) {
-        const SeqView Q = seq_view(sm, stride, g);
-        const int L = Q.L, m = L + 1;
-        const OutTabs T = out_tabs(A, sm->ws[g], L);
-        const float Z = T.F5[L];
-        float* POST = T.FMo;
-        float* dense = A.post_out ? A.post_out + A.post_offs[sm->idx[g]] : nullptr;
-        // all cells (a, b) with 0 <= a <= b <= L, walked in triangular order
-        // (thread t takes flattened cells t, t + blockDim, ...); pairs need 1 <= a < b
-        int a = threadIdx.x;
-        for (int d = 0; d <= L; ++d) {
-            const int cnt = m - d;
-            for (; a < cnt; a += blockDim.x) {
-                const int b = a + d;
-                float v = 0.0f;
-                if (a >= 1 && d >= 1) v = posterior_cell(&sm->tabs, &sm->poly, Q, T, Z, a, b);
-                POST[tri_off(d, m) + a] = v;
-                if (dense != nullptr && a >= 1) {
-                    dense[(int64_t)(a - 1) * L + (b - 1)] = v;
-                    if (d >= 1) dense[(int64_t)(b - 1) * L + (a - 1)] = 0.0f;
-                }
-            }
-            a -= cnt;
-        }
-    }
-    if (A.logz != nullptr)
-        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-            const OutTabs T = out_tabs(A, sm->ws[g], sm->L[g]);
-            A.logz[sm->idx[g]] = T.F5[sm->L[g]];
-        }
-}
-
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
 // with the reference's strict-'>' candidate order, BFS traceback.
 __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob32);
+    setup_group(sm, A, A.blob32);
     const float two_g = __fmul_rn(2.0f, A.gamma);
     // unpaired scores up[i] = (1 - sum_j POST) / (2 gamma), j ascending
     for (int g = 0; g < sm->n; ++g) {
@@ -275,7 +366,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
     }
     __syncthreads();
     wavefront(sm, 0, sm->Lmax, +1, [&](int g, int i, int j) {
-        const SeqView Q = seq_view(sm, stride, g);
+        const SeqV Q = seq_v(sm, g);
         const int m = Q.L + 1;
         const Arena32 ar = arena32(Q.L);
         float* base = A.ws + sm->ws[g];
@@ -350,7 +441,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
 // Viterbi: max-plus inside in FP64, then the reference's EPS first-match
 // traceback (cpu.py:396-501), one thread per sequence.
 // ---------------------------------------------------------------------------
-__device__ void viterbi_traceback(const SmemTabs<double>* tb, const SeqView& Q, const InTabs<double>& T,
+__device__ void viterbi_traceback(const SmemTabs<double>* tb, const SeqV& Q, const InTabs<double>& T,
                                   int* st, char* out, int* status) {
     const ParamView<double> P{tb->blob};
     const int L = Q.L;
@@ -487,8 +578,8 @@ __device__ void viterbi_traceback(const SmemTabs<double>* tb, const SeqView& Q, 
 __global__ void __launch_bounds__(kFoldThreads) k_viterbi64(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<double>*>(smem_raw);
-    const int stride = setup_group(sm, A, A.blob64);
-    inside_group<Max64>(sm, A, stride);
+    setup_group(sm, A, A.blob64);
+    inside_group<Max64>(sm, A);
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         char* out = A.structs + sm->soff[g];
@@ -496,10 +587,10 @@ __global__ void __launch_bounds__(kFoldThreads) k_viterbi64(FoldArgs A) {
     }
     __syncthreads();
     for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-        const SeqView Q = seq_view(sm, stride, g);
-        const InTabs<double> T = in_tabs<Max64>(A, sm->ws[g], Q.L);
+        const SeqV Q = seq_v(sm, g);
+        const InTabs<double> T = in_view<double>(A, sm->ws[g], Q.L).T;
         const Arena64 ar = arena64(Q.L);
-        int* st = reinterpret_cast<int*>(reinterpret_cast<double*>(A.ws + sm->ws[g]) + ar.stack);
+        int* st = reinterpret_cast<int*>(A.ws + sm->ws[g] + ar.stack);   // stack offset is in 4-byte words
         viterbi_traceback(&sm->tabs, Q, T, st, A.structs + sm->soff[g], A.status);
     }
 }
@@ -507,8 +598,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_viterbi64(FoldArgs A) {
 // ---------------------------------------------------------------------------
 size_t fold_smem_bytes(int Lmax, int group, bool fp64) {
     const size_t head = fp64 ? sizeof(SmemFold<double>) : sizeof(SmemFold<float>);
-    const size_t stride = (size_t)((Lmax + 2 + 15) & ~15);
-    return head + 2 * stride * group;
+    return head + 2 * (size_t)code_stride(Lmax) * group + (size_t)group * 4 * pb_words(Lmax) * 4;
 }
 
 }  // namespace cf

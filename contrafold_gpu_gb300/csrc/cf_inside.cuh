@@ -88,9 +88,9 @@ struct InTabs {
 };
 
 // ScoreJunctionA(i, j) for the pair (i, j+1) (cpu.py:224-228).
-template <class S>
+template <class S, class QV>
 __device__ __forceinline__ typename S::Real junctionA(const ParamView<typename S::Real>& P, int L,
-                                                      const SeqView& Q, int i, int j) {
+                                                      const QV& Q, int i, int j) {
     using R = typename S::Real;
     R jA = P.hc(Q.s[i], Q.s[j + 1]);
     if (i < L) jA = S::add(jA, P.dl(Q.s[i], Q.s[j + 1], Q.s[i + 1]));
@@ -99,9 +99,9 @@ __device__ __forceinline__ typename S::Real junctionA(const ParamView<typename S
 }
 
 // ScoreJunctionA(j, i) for the pair (i+1, j) as used by FM1 / F5 (cpu.py:237-241, 268-272).
-template <class S>
+template <class S, class QV>
 __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typename S::Real>& P, int L,
-                                                          const SeqView& Q, int i, int j) {
+                                                          const QV& Q, int i, int j) {
     using R = typename S::Real;
     R jA = P.hc(Q.s[j], Q.s[i + 1]);
     if (j < L) jA = S::add(jA, P.dl(Q.s[j], Q.s[i + 1], Q.s[j + 1]));
@@ -109,76 +109,48 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
     return jA;
 }
 
-// One inside cell (i, j).  Writes FC, FM1, FM at (i, j) (the semiring zero
-// where the reference leaves the cell at NEG).
-template <class S>
-__device__ __forceinline__ void inside_cell(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
-                                            const SeqView& Q, const InTabs<typename S::Real>& T, int i,
-                                            int j) {
+// ---------------------------------------------------------------------------
+// Two-phase cell evaluation.  On diagonal t:
+//   phase A (every cell): FM2 (kept for phase B), FM1, FM -- they read FC only
+//           up to diagonal t-2;
+//   phase B (pairable cells only): FC, which reads FC up to diagonal t-2 and the
+//           cell's own FM2.
+// The fold kernels run A(t) and B(t-1) in the same step, one barrier per step.
+// ---------------------------------------------------------------------------
+
+// Phase A of inside cell (i, j), 0 <= i <= j <= L.  Returns FM2[i][j] (the
+// semiring zero where the cell needs none).  Writes FM1, FM, and FC = zero
+// for cells that cannot close a pair (pairable cells get FC in phase B).
+template <class S, class QV>
+__device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
+                                                     const QV& Q, const InTabs<typename S::Real>& T, int i, int j) {
     using R = typename S::Real;
     const ParamView<R> P{tb->blob};
     const int L = Q.L, m = T.m, d = j - i;
     const R NEG = S::neg(), HALF = S::half();
-    const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
-    const bool fc_cell = (0 < i) && (j < L) && Q.pairable(i, j + 1);
-
+    const int at = tri_off(d, m) + i;
+    if (i == 0 || j == L) {
+        T.FC[at] = NEG;
+        T.FM1[at] = NEG;
+        T.FM[at] = NEG;
+        return NEG;
+    }
+    const bool fm_region = i + 2 <= j;
+    const bool fc_cell = Q.pairable(i, j + 1);
+    if (!fc_cell) T.FC[at] = NEG;
     // FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j]   (cpu.py:179-183)
     R fm2 = NEG;
-    if (fm_region || fc_cell) {
+    if (fm_region) {
         int o1 = tri_off(1, m) + i;          // FM1[i][i+1]
         int o2 = tri_off(d - 1, m) + i + 1;  // FM[i+1][j]
         for (int k = i + 1; k < j; ++k) {
             const R a = T.FM1[o1];
             const R b = T.FM[o2];
             if (a > HALF && b > HALF) fm2 = sr.plus(fm2, S::add(a, b));
-            const int s1 = k - i;            // span of FM1[i][k]
-            o1 += m - s1;                    // -> span s1 + 1
-            o2 += 1 - (m - (j - k - 1));     // FM[k+1][j]: span j-k-1, one position right
+            o1 += m - (k - i);
+            o2 += 1 - (m - (j - k - 1));
         }
     }
-
-    // FC[i][j], pair (i, j+1)   (cpu.py:185-230)
-    R fc = NEG;
-    if (fc_cell) {
-        const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
-        const R jB = tb->jB[idx4(si, sj1, si1, sj)];
-        R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
-        const int pmax = (i + CMAX < j) ? i + CMAX : j;
-        for (int p = i; p <= pmax; ++p) {
-            const int l1 = p - i;
-            int qmin = p + 2;
-            const int alt = l1 + j - CMAX;
-            if (alt > qmin) qmin = alt;
-            const int a = p + 1;
-            const int pca = Q.pc[a], sa = Q.s[a], sp = Q.s[p];
-            for (int q = j; q >= qmin; --q) {
-                if (!pairable_codes(pca, Q.pc[q])) continue;
-                const R inner = T.FC[tri_off(q - 1 - a, m) + a];
-                if (!(inner > HALF)) continue;
-                const int l2 = j - q;
-                R e;
-                if (l1 == 0 && l2 == 0) {
-                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
-                } else {
-                    const int sq = Q.s[q];
-                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], sp)];
-                    R snuc = R(0);
-                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
-                }
-                acc = sr.plus(acc, S::add(e, inner));
-            }
-        }
-        if (fm2 > HALF) {
-            const R jA = junctionA<S>(P, L, Q, i, j);
-            acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));
-        }
-        fc = acc;
-    }
-    T.FC[T.at(i, j)] = fc;
-
     // FM1[i][j]   (cpu.py:232-246)
     R fm1 = NEG;
     if (fm_region) {
@@ -192,8 +164,7 @@ __device__ __forceinline__ void inside_cell(const S& sr, const SmemTabs<typename
         if (ext > HALF) acc = sr.plus(acc, S::add(ext, P.mu()));
         fm1 = acc;
     }
-    T.FM1[T.at(i, j)] = fm1;
-
+    T.FM1[at] = fm1;
     // FM[i][j]   (cpu.py:248-257)
     R fm = NEG;
     if (fm_region) {
@@ -204,15 +175,76 @@ __device__ __forceinline__ void inside_cell(const S& sr, const SmemTabs<typename
         if (fm1 > HALF) acc = sr.plus(acc, fm1);
         fm = acc;
     }
-    T.FM[T.at(i, j)] = fm;
+    T.FM[at] = fm;
+    return fm2;
+}
+
+// Phase B of a pairable inside cell (i, j) (1 <= i <= j <= L-1, pair (i, j+1)):
+// FC[i][j] (cpu.py:185-230).  The single-branch candidates are the pairable
+// inner pairs (p+1, q) of the window, walked p ascending and, within a row,
+// q descending (highest set bit of the partner mask first) -- the reference's
+// order -- so only valid candidates cost work.
+template <class S, class QV>
+__device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
+                                         const QV& Q, const InTabs<typename S::Real>& T, int i, int j,
+                                         typename S::Real fm2) {
+    using R = typename S::Real;
+    const ParamView<R> P{tb->blob};
+    const int L = Q.L, m = T.m, d = j - i;
+    const R NEG = S::neg(), HALF = S::half();
+    const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
+    const R jB = tb->jB[idx4(si, sj1, si1, sj)];
+    R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
+    const int pmax = (i + CMAX < j) ? i + CMAX : j;
+    // row p = i + l1: q in [qlo, j], qlo = max(p + 2, l1 + j - 30)
+    int p = i;
+    int qlo = (p + 2 > j - CMAX) ? p + 2 : j - CMAX;
+    uint32_t msk = Q.window(p + 1, qlo, j - qlo + 1);
+    while (true) {
+        while (msk == 0u) {
+            if (++p > pmax) goto rows_done;
+            const int l1 = p - i;
+            qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
+            msk = Q.window(p + 1, qlo, j - qlo + 1);
+        }
+        {
+            const int bit = 31 - __clz(msk);
+            msk ^= 1u << bit;
+            const int q = qlo + bit;
+            const int a = p + 1;
+            const R inner = T.FC[tri_off(q - 1 - a, m) + a];
+            if (inner > HALF) {
+                const int l1 = p - i, l2 = j - q;
+                R e;
+                if (l1 == 0 && l2 == 0) {
+                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
+                } else {
+                    const int sq = Q.s[q], sa = Q.s[a];
+                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
+                    R snuc = R(0);
+                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
+                }
+                acc = sr.plus(acc, S::add(e, inner));
+            }
+        }
+    }
+rows_done:
+    if (fm2 > HALF) {
+        const R jA = junctionA<S>(P, L, Q, i, j);
+        acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));
+    }
+    T.FC[tri_off(d, m) + i] = acc;
 }
 
 // Exterior recurrence F5 (cpu.py:259-274) by one warp.  F5[j] is a sequential
 // chain over k; the lanes evaluate 32 candidate terms at a time and every lane
 // then folds them in k order (warp-uniform), so the chain is the reference's.
-template <class S>
+template <class S, class QV>
 __device__ __forceinline__ void exterior_warp(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
-                                              const SeqView& Q, const InTabs<typename S::Real>& T) {
+                                              const QV& Q, const InTabs<typename S::Real>& T) {
     using R = typename S::Real;
     const ParamView<R> P{tb->blob};
     const int L = Q.L, lane = threadIdx.x & 31;
