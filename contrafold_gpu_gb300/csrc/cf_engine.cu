@@ -16,6 +16,7 @@
 #include "../../include/contrafold_gb300.h"
 #include "cf_kernels.h"
 #include "cf_sample.h"
+#include "cf_warp.h"
 
 
 using cf::SeqDesc;
@@ -108,6 +109,9 @@ int group_for_length(int L) {
 }
 
 struct Plan {
+    bool warp = false;            // persistent warp-per-sequence kernel (batched path)
+    int wgrid = 0;                // its grid
+    int64_t slot_words = 0;       // its arena slot per warp
     std::vector<SeqDesc> descs;   // grouped order
     std::vector<int> slice_begin; // descs index where each arena slice starts (group aligned)
     std::vector<int64_t> slice_words;
@@ -136,6 +140,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         P.descs[k].seq_off = offsets[b];
         P.descs[k].L = (int)(offsets[b + 1] - offsets[b]);
         P.descs[k].idx = b;
+        P.descs[k].ws_off = 0;
     }
     // arena slices within the budget
     size_t budget = eng->budget;
@@ -145,6 +150,30 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         budget = fr / 2;
     }
     const int64_t budget_words = (int64_t)(budget / 4);
+    P.warp = batched && P.Lmax <= cf::kWarpMaxLen &&
+             (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
+    if (P.warp) {
+        // persistent grid: resident CTAs per SM x SMs, no more warps than sequences
+        const int mode = job == JOB_LOGZ ? cf::kWarpLogZ : job == JOB_MEA ? cf::kWarpMea
+                       : job == JOB_BPP ? cf::kWarpBpp : cf::kWarpSample;
+        const size_t smem = cf::warp_smem_bytes(P.Lmax);
+        int rc = ensure_smem(eng, smem);
+        if (rc) return rc;
+        int per_sm = 0, sms = 0;
+        CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cf::warp_kernel(mode), cf::kWarpThreads, smem));
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        const int wpb = cf::kWarpThreads / 32;
+        int64_t grid = (int64_t)std::max(per_sm, 1) * sms;
+        grid = std::min<int64_t>(grid, (n + wpb - 1) / wpb);
+        P.slot_words = cf::warp_slot_words(P.Lmax);
+        while (grid > 1 && grid * wpb * P.slot_words > budget_words) --grid;
+        if (grid * wpb * P.slot_words > budget_words) return fail(CF_ENOMEM, "warp arena does not fit the budget");
+        P.wgrid = (int)std::max<int64_t>(grid, 1);
+        P.group = 1;
+        P.slice_begin = {0, n};
+        P.slice_words = {grid * wpb * P.slot_words};
+        return CF_OK;
+    }
     P.slice_begin.clear();
     P.slice_words.clear();
     int64_t cur = 0;
@@ -194,6 +223,8 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     const void* ks[] = {(const void*)cf::k_inside32, (const void*)cf::k_inside32acc, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
                         (const void*)cf::k_posterior32, (const void*)cf::k_mea32, (const void*)cf::k_viterbi64};
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (int mode = 0; mode < 4; ++mode)
+        CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     eng->smem_optin = bytes;
     return CF_OK;
 }
@@ -278,6 +309,35 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
     if (X.timer) X.timer->reset();
     if (n == 0) return CF_OK;
     int rc;
+    if (P.warp) {
+        cf::WarpArgs W;
+        W.descs = X.d_descs;
+        W.n = n;
+        W.Lmax = P.Lmax;
+        W.seqs = d_seqs;
+        W.mask = d_mask;
+        W.blob32 = eng->blob32.p;
+        W.ws = X.arena;
+        W.slot_words = P.slot_words;
+        W.counter = X.status + 1;
+        W.gamma = gamma;
+        W.logz = d_logz;
+        W.structs = d_structs;
+        W.post_out = d_post;
+        W.post_offs = d_post_offs;
+        W.n_samples = sj ? sj->n_samples : 0;
+        W.seed = sj ? sj->seed : 0;
+        W.out = sj ? sj->d_out : nullptr;
+        W.status = X.status;
+        const int mode = job == JOB_LOGZ ? cf::kWarpLogZ : job == JOB_MEA ? cf::kWarpMea
+                       : job == JOB_BPP ? cf::kWarpBpp : cf::kWarpSample;
+        const size_t smem = cf::warp_smem_bytes(P.Lmax);
+        if ((rc = ensure_smem(eng, smem))) return rc;
+        CF_CUDA(cudaMemsetAsync(X.status + 1, 0, sizeof(int), st));
+        void* args[] = {&W};
+        CF_PHASE(0, (cudaLaunchKernel(cf::warp_kernel(mode), dim3(P.wgrid), dim3(cf::kWarpThreads), args, smem, st)));
+        return CF_OK;
+    }
     const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
     const size_t smem = cf::fold_smem_bytes(P.Lmax, P.group, fp64);
     if ((rc = ensure_smem(eng, smem))) return rc;
@@ -433,7 +493,7 @@ int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offset
     int64_t maxw = 1;
     for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
     if ((rc = eng->arena.ensure((size_t)maxw))) return rc;
-    if ((rc = eng->status.ensure(1))) return rc;
+    if ((rc = eng->status.ensure(2))) return rc;
     CF_CUDA(cudaMemsetAsync(eng->status.p, 0, sizeof(int), st));
     Exec X;
     X.d_descs = eng->descs.p;
@@ -588,7 +648,7 @@ int cf_plan_create(cf_engine* e, int32_t job, const int64_t* offsets, int32_t n,
     p->job = job == CF_JOB_LOGZ ? JOB_LOGZ : job == CF_JOB_LOGZ64 ? JOB_LOGZ64 : job == CF_JOB_MEA ? JOB_MEA : JOB_MFE;
     p->n = n;
     if ((rc = make_plan(e, p->job, offsets, n, p->P)) || (rc = p->descs.ensure(std::max(n, 1))) ||
-        (rc = p->status.ensure(1))) {
+        (rc = p->status.ensure(2))) {
         delete p;
         return rc;
     }

@@ -8,6 +8,7 @@
 // (flattened), so short diagonals of several sequences fill the warps that one
 // sequence alone would leave idle.  One __syncthreads separates diagonals.
 #include "cf_kernels.h"
+#include "cf_mea.cuh"
 #include "cf_outside.cuh"
 
 namespace cf {
@@ -350,56 +351,19 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
     const float two_g = __fmul_rn(2.0f, A.gamma);
-    // unpaired scores up[i] = (1 - sum_j POST) / (2 gamma), j ascending
     for (int g = 0; g < sm->n; ++g) {
-        const int L = sm->L[g], m = L + 1;
+        const int L = sm->L[g];
         const Arena32 ar = arena32(L);
         float* base = A.ws + sm->ws[g];
-        const float* POST = base + ar.FMo;
-        float* up = base + ar.up;
-        for (int i = 1 + threadIdx.x; i <= L; i += blockDim.x) {
-            float u = 1.0f;
-            for (int jj = 1; jj < i; ++jj) u = __fsub_rn(u, POST[tri_off(i - jj, m) + jj]);
-            for (int jj = i + 1; jj <= L; ++jj) u = __fsub_rn(u, POST[tri_off(jj - i, m) + i]);
-            up[i] = __fdiv_rn(u, two_g);
-        }
+        for (int i = 1 + threadIdx.x; i <= L; i += blockDim.x) base[ar.up + i] = mea_unpaired(base + ar.FMo, L, two_g, i);
     }
     __syncthreads();
     wavefront(sm, 0, sm->Lmax, +1, [&](int g, int i, int j) {
         const SeqV Q = seq_v(sm, g);
-        const int m = Q.L + 1;
         const Arena32 ar = arena32(Q.L);
         float* base = A.ws + sm->ws[g];
-        const float* POST = base + ar.FMo;
-        const float* up = base + ar.up;
-        float* score = base + ar.FM2o;
-        int* tb = reinterpret_cast<int*>(base + ar.FM);
-        const int c = tri_off(j - i, m) + i;
-        if (i == j) { score[c] = 0.0f; tb[c] = 0; return; }
-        float best = -1.0f;
-        int arg = -1;
-        float v = __fadd_rn(up[i + 1], score[tri_off(j - i - 1, m) + i + 1]);
-        if (v > best) { best = v; arg = 1; }
-        v = __fadd_rn(up[j], score[tri_off(j - 1 - i, m) + i]);
-        if (v > best) { best = v; arg = 2; }
-        if (i + 2 <= j) {
-            if (Q.pairable(i + 1, j)) {
-                v = __fadd_rn(POST[tri_off(j - i - 1, m) + i + 1], score[tri_off(j - i - 2, m) + i + 1]);
-                if (v > best) { best = v; arg = 3; }
-            }
-            int o1 = tri_off(1, m) + i;               // score[i][i+1]
-            int o2 = tri_off(j - i - 1, m) + i + 1;   // score[i+1][j]
-            for (int k = i + 1; k < j; ++k) {
-                v = __fadd_rn(score[o1], score[o2]);
-                if (v > best) { best = v; arg = k + 4; }
-                o1 += m - (k - i);
-                o2 += 1 - (m - (j - k - 1));
-            }
-        }
-        score[c] = best;
-        tb[c] = arg;
+        mea_cell(Q, base + ar.FMo, base + ar.up, base + ar.FM2o, reinterpret_cast<int*>(base + ar.FM), Q.L, i, j);
     });
-    // traceback: one thread per sequence
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         char* out = A.structs + sm->soff[g];
@@ -407,33 +371,12 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
     }
     __syncthreads();
     for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-        const int L = sm->L[g], m = L + 1;
+        const int L = sm->L[g];
         const Arena32 ar = arena32(L);
         float* base = A.ws + sm->ws[g];
-        const int* tb = reinterpret_cast<const int*>(base + ar.FM);
         int* qi = reinterpret_cast<int*>(base + ar.queue);
-        int* qj = qi + 2 * L + 4;
-        char* out = A.structs + sm->soff[g];
-        int head = 0, tail = 1;
-        qi[0] = 0; qj[0] = L;
-        while (head < tail) {
-            const int i = qi[head], j = qj[head];
-            ++head;
-            const int t = tb[tri_off(j - i, m) + i];
-            if (t <= 0) continue;
-            if (tail + 2 > 2 * L + 4) { atomicExch(A.status, CF_EDEVICE); break; }
-            if (t == 1) { qi[tail] = i + 1; qj[tail] = j; ++tail; }
-            else if (t == 2) { qi[tail] = i; qj[tail] = j - 1; ++tail; }
-            else if (t == 3) {
-                out[i] = '(';        // pair (i+1, j), 1-based
-                out[j - 1] = ')';
-                qi[tail] = i + 1; qj[tail] = j - 1; ++tail;
-            } else {
-                const int k = t - 4;
-                qi[tail] = i; qj[tail] = k; ++tail;
-                qi[tail] = k; qj[tail] = j; ++tail;
-            }
-        }
+        mea_traceback(reinterpret_cast<const int*>(base + ar.FM), L, qi, qi + 2 * L + 4, A.structs + sm->soff[g],
+                      A.status);
     }
 }
 

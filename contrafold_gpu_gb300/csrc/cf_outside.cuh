@@ -126,6 +126,55 @@ __device__ __forceinline__ void outside_A(const Lse32& sr, const SmemTabs<float>
     T.FM2o[at] = fm2o;
 }
 
+// Phase A as one loop: the FMo chain (a-1 terms) and the FM1o chain (L-1-b
+// terms) run back to back in a single loop of (a-1) + (L-1-b) = L-2-t
+// iterations, which is the same for every cell of diagonal t -- lanes of a
+// warp working on one diagonal stay converged.  Each chain keeps the
+// reference's order (see outside_A).
+__device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs<float>* __restrict__ tb,
+                                                 const SeqV& Q, const OutTabs& T, int a, int b) {
+    const ParamView<float> P{tb->blob};
+    const int L = Q.L, m = T.m, t = b - a;
+    const int at = tri_off(t, m) + a;
+    const bool fm_region = (0 < a) && (a + 2 <= b) && (b < L);
+    float fmo = CF_NEG32, fm1o = CF_NEG32;
+    if (fm_region) {
+        const int n1 = a - 1, n2 = L - 1 - b, K = n1 + n2;
+        float acc = CF_NEG32;
+        auto switch_chain = [&]() {
+            if (b + 1 < L) acc = sr.plus(acc, __fadd_rn(T.FMo[tri_off(t + 1, m) + a], P.mu()));
+            fmo = acc;
+            acc = CF_NEG32;
+            if (a >= 2) acc = sr.plus(acc, __fadd_rn(T.FM1o[tri_off(t + 1, m) + a - 1], P.mu()));
+        };
+        for (int k = 0; k < K; ++k) {
+            if (k == n1) switch_chain();
+            const bool first = k < n1;
+            const int w = first ? n1 - k : n2 - (k - n1);
+            const float* tab2 = first ? T.FM1 : T.FM;
+            const int pos1 = first ? a - w : a;
+            const int pos2 = first ? a - w : b;
+            const float src = T.FM2o[tri_off(t + w, m) + pos1];
+            const float oth = tab2[tri_off(w, m) + pos2];
+            if (src > CF_HALF32 && oth > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, oth));
+        }
+        if (K == n1) switch_chain();
+        fm1o = sr.plus(acc, fmo);
+    }
+    T.FMo[at] = fmo;
+    T.FM1o[at] = fm1o;
+    float fm2o = CF_NEG32;
+    if (fm_region) fm2o = sr.plus(fm2o, fmo);
+    if (0 < a && b < L && Q.pairable(a, b + 1)) {
+        const float fco = T.FCo[at];
+        if (fco > CF_HALF32) {
+            const float jA = junctionA<Lse32>(P, L, Q, a, b);
+            fm2o = sr.plus(fm2o, __fadd_rn(__fadd_rn(__fadd_rn(fco, jA), P.mp()), P.mb()));
+        }
+    }
+    T.FM2o[at] = fm2o;
+}
+
 // Phase B of a pairable outside cell (a, b) (pair (a, b+1)): FCo[a][b].
 //  1. exterior term of the F5o phase, k = a-1, j = b+1 (cpu.py:695-699);
 //  2. sources (i, j) = (a-1-l1, b+1+l2) of the main loop, i ascending
