@@ -108,6 +108,8 @@ int group_for_length(int L) {
     return 1;
 }
 
+int ensure_smem(cf_engine* eng, size_t bytes);
+
 struct Plan {
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
     int wgrid = 0;                // its grid
