@@ -169,12 +169,14 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         grid = std::min<int64_t>(grid, (n + wpb - 1) / wpb);
         P.slot_words = cf::warp_slot_words(P.Lmax);
         while (grid > 1 && grid * wpb * P.slot_words > budget_words) --grid;
-        if (grid * wpb * P.slot_words > budget_words) return fail(CF_ENOMEM, "warp arena does not fit the budget");
-        P.wgrid = (int)std::max<int64_t>(grid, 1);
-        P.group = 1;
-        P.slice_begin = {0, n};
-        P.slice_words = {grid * wpb * P.slot_words};
-        return CF_OK;
+        if (grid * wpb * P.slot_words <= budget_words) {
+            P.wgrid = (int)std::max<int64_t>(grid, 1);
+            P.group = 1;
+            P.slice_begin = {0, n};
+            P.slice_words = {grid * wpb * P.slot_words};
+            return CF_OK;
+        }
+        P.warp = false;   // not even one CTA of warp slots fits: per-sequence kernels, sliced
     }
     P.slice_begin.clear();
     P.slice_words.clear();
