@@ -1,0 +1,88 @@
+"""Schedule autotuner for the batched path.
+
+For each length bucket it times a synthetic MEA batch (i.i.d. ACGU, 10 %
+forced-unpaired mask) on the GPU under every schedule the engine offers --
+the persistent warp-per-sequence kernel and the persistent CTA-per-sequence
+fused kernel at 1..4 resident CTAs per SM -- and reports folds/s per choice
+and the best one per bucket.  Every schedule computes identical results; only
+speed differs.  The engine's built-in length table (cf_engine.cu,
+auto_warp_max_len / auto_ctas_per_sm) is set from these measurements.
+
+    python -m contrafold_gpu_gb300.autotune [--lengths 50,100,200,300,400] [--json out.json]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def _batch_bytes(n, L, seed):
+    rng = np.random.default_rng(seed)
+    idx = rng.integers(0, 4, size=(n, L), dtype=np.int8)
+    seq = np.frombuffer(b"ACGU", np.uint8)[idx].reshape(-1).copy()
+    mask = (rng.random((n, L)) < 0.1).astype(np.uint8).reshape(-1)
+    return seq, mask
+
+
+def time_schedule(P, L, n, kind, ctas, reps=3, job="mea"):
+    import torch
+    from .engine import CF_JOB_LOGZ, CF_JOB_MEA, Engine, Plan
+    seq, mask = _batch_bytes(n, L, 7)
+    dev = torch.device("cuda", 0)
+    d_seq = torch.from_numpy(seq).to(dev)
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_out = torch.empty(n * L if job == "mea" else 4 * n, dtype=torch.uint8, device=dev)
+    eng = Engine(P, mode="plain" if kind == "plain" else "batched")
+    if kind != "plain":
+        eng.set_schedule(kind, ctas)
+    plan = Plan(eng, CF_JOB_MEA if job == "mea" else CF_JOB_LOGZ, np.arange(n + 1, dtype=np.int64) * L)
+    stream = torch.cuda.Stream(dev)
+    plan.run(d_seq.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.run(d_seq.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    plan.status()
+    plan.close()
+    eng.close()
+    return n / (best / 1000.0)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--lengths", default="50,100,200,300,400")
+    ap.add_argument("--folds", type=float, default=2.5e10, help="work per bucket ~ folds * L^3 (sizes n)")
+    ap.add_argument("--job", default="mea", choices=["mea", "logz"])
+    ap.add_argument("--json", default=None)
+    args = ap.parse_args()
+    from . import load
+    P = load()
+    schedules = [("plain", 0), ("warp", 0), ("cta", 1), ("cta", 2), ("cta", 3), ("cta", 4)]
+    table = {}
+    for L in [int(x) for x in args.lengths.split(",")]:
+        n = int(max(304, min(20000, args.folds / L ** 3)))
+        row = {}
+        for kind, ctas in schedules:
+            t0 = time.time()
+            row[f"{kind}{ctas or ''}"] = time_schedule(P, L, n, kind, ctas, job=args.job)
+            print(f"L={L:4d} n={n:6d} {kind:5s} ctas/SM={ctas}: {row[f'{kind}{ctas or chr(32)}'.strip()] if False else row[f'{kind}{ctas or str()}']:10.1f} folds/s "
+                  f"({time.time() - t0:.1f}s)", flush=True)
+        best = max((v, k) for k, v in row.items() if k != "plain")
+        table[L] = {"n": n, "folds_per_s": row, "best": best[1], "speedup_vs_plain": best[0] / row["plain"]}
+        print(f"L={L}: best {best[1]} {best[0]:.0f} folds/s = {best[0] / row['plain']:.2f}x plain", flush=True)
+    if args.json:
+        with open(args.json, "w") as fh:
+            json.dump(table, fh, indent=1)
+    return table
+
+
+if __name__ == "__main__":
+    main()

@@ -94,6 +94,8 @@ struct cf_engine {
     DevBuf<char> samples;
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
     int mode = 1;        // 0 plain, 1 batched
+    int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent
+    int ctas_per_sm = 0; // CTA-persistent occupancy cap (0 = auto)
     size_t smem_optin = 0;
 };
 
@@ -101,6 +103,12 @@ namespace {
 
 // ---- group-size autotune table: sequences per CTA by length range ----
 // Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
+// Batched-path schedule by length (GB300 tuning): sequences up to this
+// length take the warp-per-sequence kernel for logZ/BPP/MEA.
+int auto_warp_max_len() { return 0; }
+// CTAs per SM of the persistent CTA kernel by length.
+int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 2; }
+
 int group_for_length(int L) {
     if (L <= 64) return 8;
     if (L <= 160) return 4;
@@ -111,6 +119,7 @@ int group_for_length(int L) {
 int ensure_smem(cf_engine* eng, size_t bytes);
 
 struct Plan {
+    bool cta = false;             // persistent CTA-per-sequence fused kernel (batched path)
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
     int wgrid = 0;                // its grid
     int64_t slot_words = 0;       // its arena slot per warp
@@ -152,7 +161,36 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         budget = fr / 2;
     }
     const int64_t budget_words = (int64_t)(budget / 4);
-    P.warp = batched && P.Lmax <= cf::kWarpMaxLen &&
+    // batched schedule: the fused per-sequence CTA kernel keeps only a few
+    // sequences per SM in flight (their tables stay in L2); the warp kernel
+    // runs one sequence per warp (short sequences, sampling).
+    int sched = eng->sched;
+    if (sched == 0) sched = (job == JOB_SAMPLE || P.Lmax <= auto_warp_max_len()) ? 1 : 2;
+    P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
+    if (P.cta) {
+        const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
+        const size_t smem = cf::fold_smem_bytes(P.Lmax, 1, false);
+        int rc = ensure_smem(eng, smem);
+        if (rc) return rc;
+        int per_sm = 0, sms = 0;
+        CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cf::cta_kernel(mode), cf::kFoldThreads, smem));
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        per_sm = std::max(per_sm, 1);
+        if (eng->ctas_per_sm > 0) per_sm = std::min(per_sm, eng->ctas_per_sm);
+        else per_sm = std::min(per_sm, auto_ctas_per_sm(P.Lmax));
+        int64_t grid = std::min<int64_t>((int64_t)per_sm * sms, n);
+        P.slot_words = cf::arena32(P.Lmax).total;
+        while (grid > 1 && grid * P.slot_words > budget_words) --grid;
+        if (grid * P.slot_words <= budget_words) {
+            P.wgrid = (int)std::max<int64_t>(grid, 1);
+            P.group = 1;
+            P.slice_begin = {0, n};
+            P.slice_words = {grid * P.slot_words};
+            return CF_OK;
+        }
+        P.cta = false;
+    }
+    P.warp = batched && sched == 1 && P.Lmax <= cf::kWarpMaxLen &&
              (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
     if (P.warp) {
         // persistent grid: resident CTAs per SM x SMs, no more warps than sequences
@@ -229,6 +267,8 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (int mode = 0; mode < 4; ++mode)
         CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (int mode = 0; mode < 3; ++mode)
+        CF_CUDA(cudaFuncSetAttribute(cf::cta_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     eng->smem_optin = bytes;
     return CF_OK;
 }
@@ -313,6 +353,33 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
     if (X.timer) X.timer->reset();
     if (n == 0) return CF_OK;
     int rc;
+    if (P.cta) {
+        cf::FoldArgs A;
+        A.descs = X.d_descs;
+        A.n = n;
+        A.group = 1;
+        A.seqs = d_seqs;
+        A.mask = d_mask;
+        A.blob32 = eng->blob32.p;
+        A.blob64 = eng->blob64.p;
+        A.ws = X.arena;
+        A.logz = d_logz;
+        A.logz64 = nullptr;
+        A.structs = d_structs;
+        A.post_out = d_post;
+        A.post_offs = d_post_offs;
+        A.gamma = gamma;
+        A.status = X.status;
+        const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
+        const size_t smem = cf::fold_smem_bytes(P.Lmax, 1, false);
+        if ((rc = ensure_smem(eng, smem))) return rc;
+        CF_CUDA(cudaMemsetAsync(X.status + 1, 0, sizeof(int), st));
+        int* counter = X.status + 1;
+        int64_t slot_words = P.slot_words;
+        void* args[] = {&A, &counter, &slot_words};
+        CF_PHASE(0, (cudaLaunchKernel(cf::cta_kernel(mode), dim3(P.wgrid), dim3(cf::kFoldThreads), args, smem, st)));
+        return CF_OK;
+    }
     if (P.warp) {
         cf::WarpArgs W;
         W.descs = X.d_descs;
@@ -580,6 +647,14 @@ int cf_engine_set_mode(cf_engine* e, int mode) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
     if (mode != 0 && mode != 1) return fail(CF_EINVAL, "mode must be 0 (plain) or 1 (batched)");
     e->mode = mode;
+    return CF_OK;
+}
+
+int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    if (kind < 0 || kind > 2 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
+    e->sched = kind;
+    e->ctas_per_sm = ctas_per_sm;
     return CF_OK;
 }
 

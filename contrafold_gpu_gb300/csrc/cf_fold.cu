@@ -47,6 +47,21 @@ __device__ __forceinline__ SeqV seq_v(SmemFold<R>* sm, int g) {
     return SeqV{s, pc, PB, W, sm->L[g]};
 }
 
+// Build codes and partner bit sets of the group's sequences (descriptors
+// already in shared memory).
+template <typename R>
+__device__ __forceinline__ void build_group_seqs(SmemFold<R>* sm, const FoldArgs& A) {
+    const int cs = code_stride(sm->Lmax), W = pb_words(sm->Lmax);
+    unsigned char* base = dyn_smem(sm);
+    for (int g = 0; g < sm->n; ++g) {
+        int8_t* s = reinterpret_cast<int8_t*>(base + (2 * g) * cs);
+        int8_t* pc = reinterpret_cast<int8_t*>(base + (2 * g + 1) * cs);
+        uint32_t* PB = reinterpret_cast<uint32_t*>(base + 2 * sm->gcap * cs) + (size_t)g * 4 * W;
+        build_seq(A.seqs, A.mask, sm->soff[g], sm->L[g], W, s, pc, PB);
+    }
+    __syncthreads();
+}
+
 // Load tables, group descriptors, sequence codes and partner bit sets.
 template <typename R>
 __device__ __forceinline__ void setup_group(SmemFold<R>* sm, const FoldArgs& A, const R* __restrict__ gblob) {
@@ -69,15 +84,7 @@ __device__ __forceinline__ void setup_group(SmemFold<R>* sm, const FoldArgs& A, 
     load_tabs(&sm->tabs, gblob);
     load_poly_tables(&sm->poly);
     __syncthreads();
-    const int cs = code_stride(sm->Lmax), W = pb_words(sm->Lmax);
-    unsigned char* base = dyn_smem(sm);
-    for (int g = 0; g < sm->n; ++g) {
-        int8_t* s = reinterpret_cast<int8_t*>(base + (2 * g) * cs);
-        int8_t* pc = reinterpret_cast<int8_t*>(base + (2 * g + 1) * cs);
-        uint32_t* PB = reinterpret_cast<uint32_t*>(base + 2 * sm->gcap * cs) + (size_t)g * 4 * W;
-        build_seq(A.seqs, A.mask, sm->soff[g], sm->L[g], W, s, pc, PB);
-    }
-    __syncthreads();
+    build_group_seqs(sm, A);
 }
 
 // ---------------------------------------------------------------------------
@@ -252,10 +259,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_inside64(FoldArgs A) {
 // ---------------------------------------------------------------------------
 // Outside + posterior + MEA (FP32)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    setup_group(sm, A, A.blob32);
+__device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArgs& A) {
     const Lse32 sr{&sm->poly};
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (int g = warp; g < sm->n; g += nwarps)
@@ -271,17 +275,14 @@ __global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
             },
             [&](int g, int a) {   // phase A(t): FMo, FM1o, FM2o
                 const SeqV Q = seq_v(sm, g);
-                outside_A(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t);
+                outside_A_merged(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t);
             });
     }
 }
 
 // Posterior of every pairable pair; POST goes to the FMo slot (triangular,
 // zero elsewhere) and, for cf_bpp, densely into the caller's L x L matrix.
-__global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    setup_group(sm, A, A.blob32);
+__device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldArgs& A) {
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         float* POST = out_tabs(A, sm->ws[g], L).FMo;
@@ -315,11 +316,26 @@ __global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
             c -= cnt;
         }
     }
+    __syncthreads();
     if (A.logz != nullptr)
         for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
             const OutTabs T = out_tabs(A, sm->ws[g], sm->L[g]);
             A.logz[sm->idx[g]] = T.F5[sm->L[g]];
         }
+}
+
+__global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    outside_group(sm, A);
+}
+
+__global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    posterior_group(sm, A);
 }
 
 // Walk diagonals d = d_begin .. d_end (step +1) over all sequences of the
@@ -346,10 +362,7 @@ __device__ __forceinline__ void wavefront(SmemFold<R>* sm, int d_begin, int d_en
 
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
 // with the reference's strict-'>' candidate order, BFS traceback.
-__global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
-    setup_group(sm, A, A.blob32);
+__device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A) {
     const float two_g = __fmul_rn(2.0f, A.gamma);
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
@@ -377,6 +390,75 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
         int* qi = reinterpret_cast<int*>(base + ar.queue);
         mea_traceback(reinterpret_cast<const int*>(base + ar.FM), L, qi, qi + 2 * L + 4, A.structs + sm->soff[g],
                       A.status);
+    }
+    __syncthreads();
+}
+
+// MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
+// with the reference's strict-'>' candidate order, BFS traceback.
+__global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    mea_group(sm, A);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent fused fold: each CTA takes one sequence at a time from a device
+// work queue and runs inside -> outside -> posterior -> MEA decode (or the
+// inside alone for logZ) before taking the next.  Only one or two sequences
+// per SM are in flight, so the DP tables that every diagonal step re-reads
+// stay resident in L2; the CTA's arena slot is reused across sequences.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kFoldThreads) k_fold_cta(FoldArgs A, int* counter, int64_t slot_words) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    __shared__ int item_s;
+    load_tabs(&sm->tabs, A.blob32);
+    load_poly_tables(&sm->poly);
+    const int64_t slot = (int64_t)blockIdx.x * slot_words;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int item = atomicAdd(counter, 1);
+            item_s = item;
+            if (item < A.n) {
+                const SeqDesc D = A.descs[item];
+                sm->L[0] = D.L;
+                sm->ws[0] = slot;
+                sm->soff[0] = D.seq_off;
+                sm->idx[0] = D.idx;
+                sm->n = 1;
+                sm->gcap = 1;
+                sm->Lmax = D.L;
+            }
+        }
+        __syncthreads();
+        if (item_s >= A.n) break;
+        build_group_seqs(sm, A);
+        if constexpr (MODE == kCtaLogZ) {
+            inside_group<LseAcc32>(sm, A);
+            if (threadIdx.x == 0) A.logz[sm->idx[0]] = in_view<float>(A, sm->ws[0], sm->L[0]).T.F5[sm->L[0]];
+            continue;
+        }
+        inside_group<Lse32>(sm, A);
+        outside_group(sm, A);
+        __syncthreads();
+        posterior_group(sm, A);
+        if constexpr (MODE == kCtaMea) mea_group(sm, A);
+    }
+}
+
+template __global__ void k_fold_cta<kCtaLogZ>(FoldArgs, int*, int64_t);
+template __global__ void k_fold_cta<kCtaMea>(FoldArgs, int*, int64_t);
+template __global__ void k_fold_cta<kCtaBpp>(FoldArgs, int*, int64_t);
+
+const void* cta_kernel(int mode) {
+    switch (mode) {
+        case kCtaLogZ: return (const void*)k_fold_cta<kCtaLogZ>;
+        case kCtaMea: return (const void*)k_fold_cta<kCtaMea>;
+        default: return (const void*)k_fold_cta<kCtaBpp>;
     }
 }
 

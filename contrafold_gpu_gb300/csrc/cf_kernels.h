@@ -39,4 +39,10 @@ __global__ void k_viterbi64(FoldArgs A);
 
 size_t fold_smem_bytes(int Lmax, int group, bool fp64);
 
+// Persistent fused per-sequence kernel (one CTA per sequence at a time).
+enum { kCtaLogZ = 0, kCtaMea = 1, kCtaBpp = 2 };
+template <int MODE>
+__global__ void k_fold_cta(FoldArgs A, int* counter, int64_t slot_words);
+const void* cta_kernel(int mode);
+
 }  // namespace cf

@@ -24,7 +24,7 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-           "cf_engine_set_mode", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
+           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group")
@@ -58,6 +58,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_engine_set_params.argtypes = [vp, f32p, f64p]
         L.cf_engine_set_budget.argtypes = [vp, ctypes.c_size_t]
         L.cf_engine_set_mode.argtypes = [vp, ctypes.c_int]
+        L.cf_engine_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.cf_last_error.restype = ctypes.c_char_p
         L.cf_version.restype = ctypes.c_char_p
         L.cf_logz.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f32p]
@@ -78,7 +79,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_launches.argtypes = [vp]
         L.cf_plan_group.argtypes = [vp]
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-                     "cf_engine_set_mode", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
+                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
                      "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group"):
             getattr(L, name).restype = ctypes.c_int
@@ -164,6 +165,11 @@ class Engine:
     def set_mode(self, mode: str):
         self._check(self.lib.cf_engine_set_mode(self._h, {"plain": 0, "batched": 1}[mode]))
         self.mode = mode
+
+    def set_schedule(self, kind: str = "auto", ctas_per_sm: int = 0):
+        """Batched-path schedule: 'auto', 'warp' or 'cta' (+ CTA residency cap)."""
+        self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2}[kind],
+                                                    int(ctas_per_sm)))
 
     def set_budget(self, nbytes: int):
         self._check(self.lib.cf_engine_set_budget(self._h, int(nbytes)))

@@ -89,6 +89,11 @@ int cf_engine_set_budget(cf_engine* eng, size_t bytes);
  * sequence, the reference's gpu.py:508 launch shape), 1 = batched (length-
  * bucketed groups, autotuned group size).  Results are identical. */
 int cf_engine_set_mode(cf_engine* eng, int mode);
+/* Batched-path schedule (the tuner's knob): kind 0 = automatic by length,
+ * 1 = persistent warp-per-sequence kernel, 2 = persistent CTA-per-sequence
+ * fused kernel; ctas_per_sm caps the CTA kernel's residency (0 = automatic).
+ * Results are identical for every choice. */
+int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
 
 const char* cf_last_error(void);
 const char* cf_version(void);

@@ -18,6 +18,29 @@ from conftest import golden_post, mask_of
 pytestmark = pytest.mark.gpu
 
 
+PATHS = ["plain", "warp", "cta"]
+
+
+def set_path(engine, path):
+    """plain = per-phase kernels, one sequence per CTA; warp / cta = the two
+    persistent batched kernels."""
+    if path == "plain":
+        engine.set_mode("plain")
+    else:
+        engine.set_mode("batched")
+        engine.set_schedule(path)
+
+
+@pytest.fixture(autouse=True)
+def _reset_engine(request):
+    yield
+    if "engine" in request.fixturenames:
+        eng = request.getfixturevalue("engine")
+        eng.set_mode("batched")
+        eng.set_schedule("auto")
+        eng.set_budget(0)
+
+
 def _batch(recs):
     from contrafold_gpu_gb300.engine import Batch
     return Batch([r["seq"] for r in recs], [mask_of(r) for r in recs])
@@ -43,9 +66,9 @@ def test_golden_logz64(engine, golden, mode):
         assert abs(v - r["logz64"]) <= 1e-9 * max(1.0, abs(r["logz64"])), r["seq"]
 
 
-@pytest.mark.parametrize("mode", ["plain", "batched"])
-def test_golden_logz32_tolerance(engine, golden, mode):
-    engine.set_mode(mode)
+@pytest.mark.parametrize("path", PATHS)
+def test_golden_logz32_tolerance(engine, golden, path):
+    set_path(engine, path)
     recs = golden["cases"]
     z = engine.logz(_batch(recs))
     for r, v in zip(recs, z):
@@ -53,9 +76,9 @@ def test_golden_logz32_tolerance(engine, golden, mode):
         assert err <= 5e-4, (r["seq"], err)
 
 
-@pytest.mark.parametrize("mode", ["plain", "batched"])
-def test_golden_bpp_bitwise(engine, golden, mode):
-    engine.set_mode(mode)
+@pytest.mark.parametrize("path", PATHS)
+def test_golden_bpp_bitwise(engine, golden, path):
+    set_path(engine, path)
     recs = golden["cases"]
     mats, _ = engine.bpp(_batch(recs))
     for r, M in zip(recs, mats):
@@ -68,9 +91,9 @@ def test_golden_bpp_bitwise(engine, golden, mode):
             assert np.array_equal(ref.view(np.uint32), M.view(np.uint32))
 
 
-@pytest.mark.parametrize("mode", ["plain", "batched"])
-def test_golden_mea(engine, golden, mode):
-    engine.set_mode(mode)
+@pytest.mark.parametrize("path", PATHS)
+def test_golden_mea(engine, golden, path):
+    set_path(engine, path)
     recs = golden["cases"]
     gammas = sorted({g for r in recs for g in r["mea"]}, key=float)
     for g in gammas:
@@ -118,12 +141,18 @@ def test_plain_equals_batched(engine):
     seqs, masks = _rand_batch(5, 97, 1, 260, 0.1)
     B = Batch(seqs, masks)
     res = {}
-    for mode in ("plain", "batched"):
-        engine.set_mode(mode)
-        res[mode] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B))
-    assert np.array_equal(res["plain"][0], res["batched"][0])
-    assert res["plain"][1] == res["batched"][1]
-    assert res["plain"][2] == res["batched"][2]
+    for path in PATHS:
+        set_path(engine, path)
+        mats, z = engine.bpp(B)
+        res[path] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B), z, np.concatenate([m.ravel() for m in mats]))
+    set_path(engine, "cta")
+    engine.set_schedule("auto")
+    for path in ("warp", "cta"):
+        assert np.array_equal(res["plain"][0], res[path][0])
+        assert res["plain"][1] == res[path][1]
+        assert res["plain"][2] == res[path][2]
+        assert np.array_equal(res["plain"][3], res[path][3])
+        assert np.array_equal(res["plain"][4].view(np.uint32), res[path][4].view(np.uint32))
 
 
 def test_edge_cases(engine, P, oracle):
