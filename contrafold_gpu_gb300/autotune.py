@@ -72,9 +72,9 @@ def main():
         row = {}
         for kind, ctas in schedules:
             t0 = time.time()
-            row[f"{kind}{ctas or ''}"] = time_schedule(P, L, n, kind, ctas, job=args.job)
-            print(f"L={L:4d} n={n:6d} {kind:5s} ctas/SM={ctas}: {row[f'{kind}{ctas or chr(32)}'.strip()] if False else row[f'{kind}{ctas or str()}']:10.1f} folds/s "
-                  f"({time.time() - t0:.1f}s)", flush=True)
+            key = f"{kind}{ctas}" if ctas else kind
+            row[key] = time_schedule(P, L, n, kind, ctas, job=args.job)
+            print(f"L={L:4d} n={n:6d} {key:6s}: {row[key]:10.1f} folds/s ({time.time() - t0:.1f}s)", flush=True)
         best = max((v, k) for k, v in row.items() if k != "plain")
         table[L] = {"n": n, "folds_per_s": row, "best": best[1], "speedup_vs_plain": best[0] / row["plain"]}
         print(f"L={L}: best {best[1]} {best[0]:.0f} folds/s = {best[0] / row['plain']:.2f}x plain", flush=True)
