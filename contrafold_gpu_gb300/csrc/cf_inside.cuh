@@ -110,6 +110,38 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 }
 
 // ---------------------------------------------------------------------------
+// Prefetched sequential chains.  A bifurcation chain folds n terms x_k * y_k
+// (k ascending) into an accumulator; each step depends on the previous one,
+// but the operand loads do not.  The loop below keeps a rolling register
+// pipeline of 2*PF terms: the loads of block b+1 are issued before block b is
+// folded, so global-memory latency overlaps the dependent log-sum-exp chain
+// instead of stalling every step.  `ld(x, y)` loads the next term in k order
+// (it carries its own incremental addressing); `step(k, x, y)` folds term k.
+// ---------------------------------------------------------------------------
+constexpr int kChainPF = 4;
+
+template <typename R, class Ld, class Step>
+__device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
+    R xa[kChainPF], ya[kChainPF], xb[kChainPF], yb[kChainPF];
+#pragma unroll
+    for (int u = 0; u < kChainPF; ++u)
+        if (u < n) ld(xa[u], ya[u]);
+    for (int k0 = 0; k0 < n; k0 += kChainPF) {
+#pragma unroll
+        for (int u = 0; u < kChainPF; ++u)
+            if (k0 + kChainPF + u < n) ld(xb[u], yb[u]);
+#pragma unroll
+        for (int u = 0; u < kChainPF; ++u)
+            if (k0 + u < n) step(k0 + u, xa[u], ya[u]);
+#pragma unroll
+        for (int u = 0; u < kChainPF; ++u) {
+            xa[u] = xb[u];
+            ya[u] = yb[u];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Two-phase cell evaluation.  On diagonal t:
 //   phase A (every cell): FM2 (kept for phase B), FM1, FM -- they read FC only
 //           up to diagonal t-2;
@@ -141,15 +173,23 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
     // FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j]   (cpu.py:179-183)
     R fm2 = NEG;
     if (fm_region) {
+        // term k = i+1 .. j-1: FM1[i][k] (span s1 = k-i), FM[k][j] (span s2 = j-k)
         int o1 = tri_off(1, m) + i;          // FM1[i][i+1]
         int o2 = tri_off(d - 1, m) + i + 1;  // FM[i+1][j]
-        for (int k = i + 1; k < j; ++k) {
-            const R a = T.FM1[o1];
-            const R b = T.FM[o2];
-            if (a > HALF && b > HALF) fm2 = sr.plus(fm2, S::add(a, b));
-            o1 += m - (k - i);
-            o2 += 1 - (m - (j - k - 1));
-        }
+        int s1 = 1, s2 = d - 1;
+        prefetched_chain<R>(
+            d - 1,
+            [&](R& x, R& y) {
+                x = T.FM1[o1];
+                y = T.FM[o2];
+                o1 += m - s1;
+                o2 += s2 - m;           // FM[k+1][j]: span s2-1, one position right
+                ++s1;
+                --s2;
+            },
+            [&](int, R x, R y) {
+                if (x > HALF && y > HALF) fm2 = sr.plus(fm2, S::add(x, y));
+            });
     }
     // FM1[i][j]   (cpu.py:232-246)
     R fm1 = NEG;
@@ -196,42 +236,54 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
     const R jB = tb->jB[idx4(si, sj1, si1, sj)];
     R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
     const int pmax = (i + CMAX < j) ? i + CMAX : j;
-    // row p = i + l1: q in [qlo, j], qlo = max(p + 2, l1 + j - 30)
-    int p = i;
-    int qlo = (p + 2 > j - CMAX) ? p + 2 : j - CMAX;
-    uint32_t msk = Q.window(p + 1, qlo, j - qlo + 1);
-    while (true) {
-        while (msk == 0u) {
-            if (++p > pmax) goto rows_done;
-            const int l1 = p - i;
-            qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
-            msk = Q.window(p + 1, qlo, j - qlo + 1);
+    // Candidate generator: row p = i + l1 (ascending), q in [qlo, j] with
+    // qlo = max(p + 2, l1 + j - 30), pairable inner pairs (p+1, q) from the
+    // partner mask, highest q first.  Two candidates are kept in flight so the
+    // inner-value loads overlap the log-sum-exp of the current candidate.
+    int gp = i;
+    int gqlo = (gp + 2 > j - CMAX) ? gp + 2 : j - CMAX;
+    uint32_t gmsk = Q.window(gp + 1, gqlo, j - gqlo + 1);
+    auto gen = [&](int& pp, int& qq) -> bool {
+        while (gmsk == 0u) {
+            if (++gp > pmax) return false;
+            const int l1 = gp - i;
+            gqlo = (gp + 2 > l1 + j - CMAX) ? gp + 2 : l1 + j - CMAX;
+            gmsk = Q.window(gp + 1, gqlo, j - gqlo + 1);
         }
-        {
-            const int bit = 31 - __clz(msk);
-            msk ^= 1u << bit;
-            const int q = qlo + bit;
-            const int a = p + 1;
-            const R inner = T.FC[tri_off(q - 1 - a, m) + a];
-            if (inner > HALF) {
-                const int l1 = p - i, l2 = j - q;
-                R e;
-                if (l1 == 0 && l2 == 0) {
-                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
-                } else {
-                    const int sq = Q.s[q], sa = Q.s[a];
-                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
-                    R snuc = R(0);
-                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
-                }
-                acc = sr.plus(acc, S::add(e, inner));
+        const int bit = 31 - __clz(gmsk);
+        gmsk ^= 1u << bit;
+        pp = gp;
+        qq = gqlo + bit;
+        return true;
+    };
+    auto ld = [&](int pp, int qq) -> R { return T.FC[tri_off(qq - 2 - pp, m) + pp + 1]; };
+    int p0 = 0, q0 = 0, p1 = 0, q1 = 0, p2 = 0, q2 = 0;
+    bool h0 = gen(p0, q0);
+    R v0 = h0 ? ld(p0, q0) : R(0);
+    bool h1 = h0 && gen(p1, q1);
+    R v1 = h1 ? ld(p1, q1) : R(0);
+    while (h0) {
+        const bool h2 = h1 && gen(p2, q2);
+        const R v2 = h2 ? ld(p2, q2) : R(0);
+        if (v0 > HALF) {
+            const int l1 = p0 - i, l2 = j - q0, a = p0 + 1;
+            R e;
+            if (l1 == 0 && l2 == 0) {
+                e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
+            } else {
+                const int sq = Q.s[q0], sa = Q.s[a];
+                const R jB2 = tb->jB[idx4(sq, sa, Q.s[q0 + 1], Q.s[p0])];
+                R snuc = R(0);
+                if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
             }
+            acc = sr.plus(acc, S::add(e, v0));
         }
+        p0 = p1; q0 = q1; v0 = v1; h0 = h1;
+        p1 = p2; q1 = q2; v1 = v2; h1 = h2;
     }
-rows_done:
     if (fm2 > HALF) {
         const R jA = junctionA<S>(P, L, Q, i, j);
         acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));

@@ -8,7 +8,7 @@
 // reference's; traceback order does not affect the result.
 #pragma once
 
-#include "cf_device.cuh"
+#include "cf_inside.cuh"
 
 namespace cf {
 
@@ -44,14 +44,24 @@ __device__ __forceinline__ void mea_cell(const QV& Q, const float* __restrict__ 
             v = __fadd_rn(POST[tri_off(j - i - 1, m) + i + 1], score[tri_off(j - i - 2, m) + i + 1]);
             if (v > best) { best = v; arg = 3; }
         }
+        // bifurcations k = i+1 .. j-1: score[i][k] (span s1 = k-i), score[k][j] (span s2 = j-k)
         int o1 = tri_off(1, m) + i;               // score[i][i+1]
         int o2 = tri_off(j - i - 1, m) + i + 1;   // score[i+1][j]
-        for (int k = i + 1; k < j; ++k) {
-            v = __fadd_rn(score[o1], score[o2]);
-            if (v > best) { best = v; arg = k + 4; }
-            o1 += m - (k - i);
-            o2 += 1 - (m - (j - k - 1));
-        }
+        int s1 = 1, s2 = j - i - 1;
+        prefetched_chain<float>(
+            j - i - 1,
+            [&](float& x, float& y) {
+                x = score[o1];
+                y = score[o2];
+                o1 += m - s1;
+                o2 += s2 - m;
+                ++s1;
+                --s2;
+            },
+            [&](int k, float x, float y) {
+                const float vv = __fadd_rn(x, y);
+                if (vv > best) { best = vv; arg = i + 1 + k + 4; }
+            });
     }
     score[c] = best;
     tb[c] = arg;

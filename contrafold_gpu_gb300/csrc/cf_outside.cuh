@@ -147,17 +147,33 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
             acc = CF_NEG32;
             if (a >= 2) acc = sr.plus(acc, __fadd_rn(T.FM1o[tri_off(t + 1, m) + a - 1], P.mu()));
         };
-        for (int k = 0; k < K; ++k) {
-            if (k == n1) switch_chain();
-            const bool first = k < n1;
-            const int w = first ? n1 - k : n2 - (k - n1);
-            const float* tab2 = first ? T.FM1 : T.FM;
-            const int pos1 = first ? a - w : a;
-            const int pos2 = first ? a - w : b;
-            const float src = T.FM2o[tri_off(t + w, m) + pos1];
-            const float oth = tab2[tri_off(w, m) + pos2];
-            if (src > CF_HALF32 && oth > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, oth));
-        }
+        // loader: phase 1 (k < n1) reads FM2o[a-w][b], FM1[a-w][a] with w = n1-k;
+        // phase 2 reads FM2o[a][b+w], FM[b][b+w] with w = n2-(k-n1)
+        int kl = 0, w = n1;
+        int addr1 = tri_off(t + n1, m) + a - n1, addr2 = tri_off(n1, m) + a - n1;
+        const float* tab2 = T.FM1;
+        int first = 1;
+        prefetched_chain<float>(
+            K,
+            [&](float& x, float& y) {
+                if (kl == n1) {
+                    w = n2;
+                    addr1 = tri_off(t + n2, m) + a;
+                    addr2 = tri_off(n2, m) + b;
+                    tab2 = T.FM;
+                    first = 0;
+                }
+                x = T.FM2o[addr1];
+                y = tab2[addr2];
+                addr1 -= (m - t - w + 1) - first;
+                addr2 -= (m - w + 1) - first;
+                --w;
+                ++kl;
+            },
+            [&](int k, float x, float y) {
+                if (k == n1) switch_chain();
+                if (x > CF_HALF32 && y > CF_HALF32) acc = sr.plus(acc, __fadd_rn(x, y));
+            });
         if (K == n1) switch_chain();
         fm1o = sr.plus(acc, fmo);
     }
@@ -201,61 +217,80 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
     // jB of the inner pair (p+1, q) = (a, b+1): hc[s[q]][s[p+1]] + tm[s[q]][s[p+1]][s[q+1]][s[p]]
     const float jB2 = tb->jB[idx4(sb1, sa, Q.s[b + 2], Q.s[a - 1])];
     const int l1max = (a - 2 < CMAX) ? a - 2 : CMAX;   // i = a-1-l1 >= 1
-    for (int l1 = l1max; l1 >= 0; --l1) {
-        const int i = a - 1 - l1;
-        // sources j = b+1 .. min(L-1, b+1+30-l1); mask bit k <-> j+1 = b+2+k
+    // Generator over (kind, l1, j): rows l1 = l1max .. 0, j descending within a
+    // row (highest mask bit first); in row 0 the FM1o term of source
+    // (a-1, b+1) (kind 1) comes after the l2 >= 1 candidates and before l2 = 0.
+    int gl1 = l1max;
+    uint32_t gmsk = 0u;
+    bool ev_pending = false, bit0_pending = false;
+    auto rowmask = [&](int l1) -> uint32_t {
         const int jmax = (b + 1 + CMAX - l1 < L - 1) ? b + 1 + CMAX - l1 : L - 1;
-        uint32_t msk = Q.window(i, b + 2, jmax - (b + 1) + 1);
-        if (l1 == 0) {
-            // bits for l2 >= 1 first, then the FM1o term of source (a-1, b+1), then l2 = 0
-            const uint32_t rest = msk & ~1u;
-            msk &= 1u;
-            uint32_t r = rest;
-            while (r) {
-                const int bit = 31 - __clz(r);
-                r ^= 1u << bit;
-                const int j = b + 1 + bit;
-                const float src = T.FCo[tri_off(j - i, m) + i];
-                if (src > CF_HALF32) {
-                    const int l2 = bit, sj = Q.s[j], si1 = Q.s[i + 1];
-                    const float jBij = tb->jB[idx4(Q.s[i], Q.s[j + 1], si1, sj)];
-                    float snuc = 0.0f;
-                    if (l2 == 1) snuc = P.b01(sj);
-                    const float e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(0, l2), bp_ab), jBij), jB2), snuc);
-                    acc = sr.plus(acc, __fadd_rn(src, e));
-                }
-            }
-            if (b + 1 < L) {   // source (a-1, b+1) exists (j = b+1 <= L-1); a >= 2 since l1max >= 0
-                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
-                acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(T.FM1o[tri_off(t + 2, m) + a - 1], jAji), P.mp()), bp_ab));
-            }
-            if (msk) {
-                const int j = b + 1;
-                const float src = T.FCo[tri_off(j - i, m) + i];
-                if (src > CF_HALF32) {
-                    const int si1 = Q.s[i + 1], sj = Q.s[j];
-                    const float e = __fadd_rn(P.bp(si1, sj), P.stack(Q.s[i], Q.s[j + 1], si1, sj));
-                    acc = sr.plus(acc, __fadd_rn(src, e));
-                }
-            }
+        return Q.window(a - 1 - l1, b + 2, jmax - b);
+    };
+    auto enter_row = [&]() {
+        const uint32_t m0 = rowmask(gl1);
+        if (gl1 == 0) {
+            gmsk = m0 & ~1u;
+            ev_pending = b + 1 < L;
+            bit0_pending = (m0 & 1u) != 0u;
         } else {
-            const int si = Q.s[i], si1 = Q.s[i + 1];
-            while (msk) {
-                const int bit = 31 - __clz(msk);
-                msk ^= 1u << bit;
-                const int j = b + 1 + bit;
-                const float src = T.FCo[tri_off(j - i, m) + i];
-                if (src > CF_HALF32) {
-                    const int l2 = bit, sj = Q.s[j];
-                    const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
-                    float snuc = 0.0f;
-                    if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                    const float e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), bp_ab), jBij), jB2), snuc);
-                    acc = sr.plus(acc, __fadd_rn(src, e));
-                }
-            }
+            gmsk = m0;
         }
+    };
+    if (gl1 >= 0) enter_row();
+    auto gen = [&](int& kind, int& l1, int& j) -> bool {
+        if (gl1 < 0) return false;
+        while (true) {
+            if (gmsk) {
+                const int bit = 31 - __clz(gmsk);
+                gmsk ^= 1u << bit;
+                kind = 0; l1 = gl1; j = b + 1 + bit;
+                return true;
+            }
+            if (gl1 == 0) {
+                if (ev_pending) { ev_pending = false; kind = 1; l1 = 0; j = b + 1; return true; }
+                if (bit0_pending) { bit0_pending = false; kind = 0; l1 = 0; j = b + 1; return true; }
+                gl1 = -1;
+                return false;
+            }
+            --gl1;
+            enter_row();
+        }
+    };
+    auto ld = [&](int kind, int l1, int j) -> float {
+        if (kind == 1) return T.FM1o[tri_off(t + 2, m) + a - 1];
+        const int i = a - 1 - l1;
+        return T.FCo[tri_off(j - i, m) + i];
+    };
+    int k0 = 0, l10 = 0, j0 = 0, k1 = 0, l11 = 0, j1 = 0, k2 = 0, l12 = 0, j2 = 0;
+    bool h0 = gen(k0, l10, j0);
+    float v0 = h0 ? ld(k0, l10, j0) : 0.0f;
+    bool h1 = h0 && gen(k1, l11, j1);
+    float v1 = h1 ? ld(k1, l11, j1) : 0.0f;
+    while (h0) {
+        const bool h2 = h1 && gen(k2, l12, j2);
+        const float v2 = h2 ? ld(k2, l12, j2) : 0.0f;
+        if (k0 == 1) {
+            const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
+            acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v0, jAji), P.mp()), bp_ab));
+        } else if (v0 > CF_HALF32) {
+            const int i = a - 1 - l10, l2 = j0 - (b + 1);
+            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j0];
+            float e;
+            if (l10 == 0 && l2 == 0) {
+                e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[j0 + 1], si1, sj));
+            } else {
+                const float jBij = tb->jB[idx4(si, Q.s[j0 + 1], si1, sj)];
+                float snuc = 0.0f;
+                if (l10 == 0 && l2 == 1) snuc = P.b01(sj);
+                else if (l10 == 1 && l2 == 0) snuc = P.b01(si1);
+                else if (l10 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l10, l2), bp_ab), jBij), jB2), snuc);
+            }
+            acc = sr.plus(acc, __fadd_rn(v0, e));
+        }
+        k0 = k1; l10 = l11; j0 = j1; v0 = v1; h0 = h1;
+        k1 = k2; l11 = l12; j1 = j2; v1 = v2; h1 = h2;
     }
     T.FCo[tri_off(t, m) + a] = acc;
 }
@@ -278,45 +313,78 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
     const float jB2 = tb->jB[idx4(sb, sa, Q.s[b + 1], Q.s[a - 1])];
     float post = 0.0f;
     const int l1max = (a - 2 < CMAX) ? a - 2 : CMAX;   // i = a-1-l1 >= 1
-    for (int l1 = 0; l1 <= l1max; ++l1) {
-        const int i = a - 1 - l1;
-        const int si = Q.s[i], si1 = Q.s[i + 1];
-        // sources j = b .. min(L-1, b+30-l1); mask bit k <-> j+1 = b+1+k
+    // Generator over (kind, l1, j): rows l1 = 0 .. l1max, j ascending within a
+    // row (lowest mask bit first); in row 0 the multiloop term of source
+    // (a-1, b) (kind 1) follows that source's stacking term (l2 = 0).
+    int gl1 = 0;
+    uint32_t gmsk = 0u;
+    bool ev_pending = false, bit0_pending = false;
+    auto rowmask = [&](int l1) -> uint32_t {
         const int jmax = (b + CMAX - l1 < L - 1) ? b + CMAX - l1 : L - 1;
-        uint32_t msk = Q.window(i, b + 1, jmax - b + 1);
-        bool fm1_pending = (l1 == 0) && (b < L);
-        while (msk || fm1_pending) {
-            const int bit = msk ? __ffs(msk) - 1 : 32;
-            if (fm1_pending && bit > 0) {
-                // multiloop term of source (a-1, b): after its own stacking term (bit 0)
-                fm1_pending = false;
-                const float fo = T.FM1o[tri_off(b - a + 1, m) + a - 1];
-                if (fo > CF_HALF32) {
-                    const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
-                    const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(fo, fcin), jAji), P.mp()), bp_ab), Z);
-                    post = __fadd_rn(post, fexp32(pt, x));
-                }
-                continue;
+        return Q.window(a - 1 - l1, b + 1, jmax - b + 1);
+    };
+    if (l1max >= 0) {
+        const uint32_t m0 = rowmask(0);
+        bit0_pending = (m0 & 1u) != 0u;
+        ev_pending = b < L;
+        gmsk = m0 & ~1u;
+    } else {
+        gl1 = 1;   // no rows
+    }
+    auto gen = [&](int& kind, int& l1, int& j) -> bool {
+        while (true) {
+            if (gl1 == 0 && bit0_pending) { bit0_pending = false; kind = 0; l1 = 0; j = b; return true; }
+            if (gl1 == 0 && ev_pending) { ev_pending = false; kind = 1; l1 = 0; j = b; return true; }
+            if (gmsk) {
+                const int bit = __ffs(gmsk) - 1;
+                gmsk &= gmsk - 1u;
+                kind = 0; l1 = gl1; j = b + bit;
+                return true;
             }
-            msk &= msk - 1;
-            const int j = b + bit, l2 = bit;
-            const float outside = __fsub_rn(T.FCo[tri_off(j - i, m) + i], Z);
+            if (++gl1 > l1max) return false;
+            gmsk = rowmask(gl1);
+        }
+    };
+    auto ld = [&](int kind, int l1, int j) -> float {
+        if (kind == 1) return T.FM1o[tri_off(b - a + 1, m) + a - 1];
+        const int i = a - 1 - l1;
+        return T.FCo[tri_off(j - i, m) + i];
+    };
+    int k0 = 0, l10 = 0, j0 = 0, k1 = 0, l11 = 0, j1 = 0, k2 = 0, l12 = 0, j2 = 0;
+    bool h0 = gen(k0, l10, j0);
+    float v0 = h0 ? ld(k0, l10, j0) : 0.0f;
+    bool h1 = h0 && gen(k1, l11, j1);
+    float v1 = h1 ? ld(k1, l11, j1) : 0.0f;
+    while (h0) {
+        const bool h2 = h1 && gen(k2, l12, j2);
+        const float v2 = h2 ? ld(k2, l12, j2) : 0.0f;
+        if (k0 == 1) {
+            if (v0 > CF_HALF32) {
+                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
+                const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v0, fcin), jAji), P.mp()), bp_ab), Z);
+                post = __fadd_rn(post, fexp32(pt, x));
+            }
+        } else {
+            const float outside = __fsub_rn(v0, Z);
             if (outside > CF_HALF32) {
-                const int sj = Q.s[j];
+                const int i = a - 1 - l10, l2 = j0 - b;
+                const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j0];
                 float e;
-                if (l1 == 0 && l2 == 0) {
-                    e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j + 1], si1, sj)), fcin);
+                if (l10 == 0 && l2 == 0) {
+                    e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j0 + 1], si1, sj)), fcin);
                 } else {
-                    const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
+                    const float jBij = tb->jB[idx4(si, Q.s[j0 + 1], si1, sj)];
                     float snuc = 0.0f;
-                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                    e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l1, l2)), fcin), bp_ab), jB2), snuc);
+                    if (l10 == 0 && l2 == 1) snuc = P.b01(sj);
+                    else if (l10 == 1 && l2 == 0) snuc = P.b01(si1);
+                    else if (l10 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                    e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l10, l2)), fcin), bp_ab), jB2), snuc);
                 }
                 post = __fadd_rn(post, fexp32(pt, e));
             }
         }
+        k0 = k1; l10 = l11; j0 = j1; v0 = v1; h0 = h1;
+        k1 = k2; l11 = l12; j1 = j2; v1 = v2; h1 = h2;
     }
     const float outside = __fsub_rn(T.F5o[b], Z);
     const float f5k = T.F5[a - 1];
