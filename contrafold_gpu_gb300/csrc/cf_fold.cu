@@ -226,7 +226,7 @@ __device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, con
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kFoldThreads) k_inside32(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_inside32(FoldArgs A) {
 }
 
 // Same recurrence with accurate float32 log-sum-exp: logZ_batch and the sampler.
-__global__ void __launch_bounds__(kFoldThreads) k_inside32acc(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside32acc(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_inside32acc(FoldArgs A) {
             A.logz[sm->idx[g]] = in_view<float>(A, sm->ws[g], sm->L[g]).T.F5[sm->L[g]];
 }
 
-__global__ void __launch_bounds__(kFoldThreads) k_inside64(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside64(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<double>*>(smem_raw);
     setup_group(sm, A, A.blob64);
@@ -324,14 +324,14 @@ __device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldA
         }
 }
 
-__global__ void __launch_bounds__(kFoldThreads) k_outside32(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_outside32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
     outside_group(sm, A);
 }
 
-__global__ void __launch_bounds__(kFoldThreads) k_posterior32(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_posterior32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -396,7 +396,7 @@ __device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A
 
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
 // with the reference's strict-'>' candidate order, BFS traceback.
-__global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_mea32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_mea32(FoldArgs A) {
 // stay resident in L2; the CTA's arena slot is reused across sequences.
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kFoldThreads) k_fold_cta(FoldArgs A, int* counter, int64_t slot_words) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_fold_cta(FoldArgs A, int* counter, int64_t slot_words) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     __shared__ int item_s;
@@ -600,7 +600,7 @@ __device__ void viterbi_traceback(const SmemTabs<double>* tb, const SeqV& Q, con
 #undef VPUSH
 }
 
-__global__ void __launch_bounds__(kFoldThreads) k_viterbi64(FoldArgs A) {
+__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_viterbi64(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<double>*>(smem_raw);
     setup_group(sm, A, A.blob64);

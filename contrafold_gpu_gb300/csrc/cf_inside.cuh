@@ -188,7 +188,12 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
                 --s2;
             },
             [&](int, R x, R y) {
-                if (x > HALF && y > HALF) fm2 = sr.plus(fm2, S::add(x, y));
+                // Terms with an operand at the zero sentinel are skipped by the
+                // reference; here they are folded unconditionally (no divergent
+                // branch): such a term is <= NEG and every semiring's plus keeps
+                // the accumulator -- or, from the NEG start, yields another
+                // sub-HALF value, which all readers of FM2 treat as zero.
+                fm2 = sr.plus(fm2, S::add(x, y));
             });
     }
     // FM1[i][j]   (cpu.py:232-246)

@@ -9,6 +9,7 @@
 namespace cf {
 
 constexpr int kFoldThreads = 256;   // threads per fold CTA
+constexpr int kFoldMinBlocks = 3;   // resident CTAs per SM the register budget targets
 constexpr int kMaxGroup = 32;       // sequences per CTA on the batched path
 
 struct FoldArgs {

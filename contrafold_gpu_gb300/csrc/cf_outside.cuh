@@ -172,7 +172,9 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
             },
             [&](int k, float x, float y) {
                 if (k == n1) switch_chain();
-                if (x > CF_HALF32 && y > CF_HALF32) acc = sr.plus(acc, __fadd_rn(x, y));
+                // unguarded fold: a sentinel operand makes the term <= NEG, which
+                // Fast_LogPlusEquals discards (it returns the larger argument)
+                acc = sr.plus(acc, __fadd_rn(x, y));
             });
         if (K == n1) switch_chain();
         fm1o = sr.plus(acc, fmo);

@@ -195,7 +195,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarpThreads) k_fold_warp(WarpArgs A) {
+__global__ void __launch_bounds__(kWarpThreads, 3) k_fold_warp(WarpArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<WarpSmemHead*>(smem_raw);
     load_tabs(&sm->tabs, A.blob32);
