@@ -105,9 +105,9 @@ namespace {
 // Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
 // Batched-path schedule by length (GB300 tuning): sequences up to this
 // length take the warp-per-sequence kernel for logZ/BPP/MEA.
-int auto_warp_max_len() { return 0; }
+int auto_warp_max_len() { return 320; }
 // CTAs per SM of the persistent CTA kernel by length.
-int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 2; }
+int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
 
 int group_for_length(int L) {
     if (L <= 64) return 8;

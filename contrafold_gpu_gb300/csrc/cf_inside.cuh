@@ -118,25 +118,66 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 // instead of stalling every step.  `ld(x, y)` loads the next term in k order
 // (it carries its own incremental addressing); `step(k, x, y)` folds term k.
 // ---------------------------------------------------------------------------
-constexpr int kChainPF = 4;
+// Prefetch depths are per translation unit (each .cu file is its own device
+// module, compiled without relocatable device code): CF_CHAIN_PF terms per
+// pipeline block (0 = plain load-then-fold loop) and CF_WINDOW_LOOKAHEAD
+// window candidates in flight (0 or 2).
+#ifndef CF_CHAIN_PF
+#define CF_CHAIN_PF 4
+#endif
+#ifndef CF_WINDOW_LOOKAHEAD
+#define CF_WINDOW_LOOKAHEAD 2
+#endif
+constexpr int kChainPF = CF_CHAIN_PF;
 
 template <typename R, class Ld, class Step>
 __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
-    R xa[kChainPF], ya[kChainPF], xb[kChainPF], yb[kChainPF];
-#pragma unroll
-    for (int u = 0; u < kChainPF; ++u)
-        if (u < n) ld(xa[u], ya[u]);
-    for (int k0 = 0; k0 < n; k0 += kChainPF) {
+    if constexpr (kChainPF == 0) {
+        for (int k = 0; k < n; ++k) {
+            R x, y;
+            ld(x, y);
+            step(k, x, y);
+        }
+    } else {
+        R xa[kChainPF], ya[kChainPF], xb[kChainPF], yb[kChainPF];
 #pragma unroll
         for (int u = 0; u < kChainPF; ++u)
-            if (k0 + kChainPF + u < n) ld(xb[u], yb[u]);
+            if (u < n) ld(xa[u], ya[u]);
+        for (int k0 = 0; k0 < n; k0 += kChainPF) {
 #pragma unroll
-        for (int u = 0; u < kChainPF; ++u)
-            if (k0 + u < n) step(k0 + u, xa[u], ya[u]);
+            for (int u = 0; u < kChainPF; ++u)
+                if (k0 + kChainPF + u < n) ld(xb[u], yb[u]);
 #pragma unroll
-        for (int u = 0; u < kChainPF; ++u) {
-            xa[u] = xb[u];
-            ya[u] = yb[u];
+            for (int u = 0; u < kChainPF; ++u)
+                if (k0 + u < n) step(k0 + u, xa[u], ya[u]);
+#pragma unroll
+            for (int u = 0; u < kChainPF; ++u) {
+                xa[u] = xb[u];
+                ya[u] = yb[u];
+            }
+        }
+    }
+}
+
+// Drive a candidate generator `gen(c) -> bool`, loading each candidate with
+// `ld(c)` CF_WINDOW_LOOKAHEAD candidates ahead of `use(c, value)`.
+template <typename R, class C, class Gen, class Ld, class Use>
+__device__ __forceinline__ void lookahead_walk(Gen gen, Ld ld, Use use) {
+    if constexpr (CF_WINDOW_LOOKAHEAD == 0) {
+        C c;
+        while (gen(c)) use(c, ld(c));
+    } else {
+        C c0, c1, c2;
+        bool h0 = gen(c0);
+        R v0 = h0 ? ld(c0) : R(0);
+        bool h1 = h0 && gen(c1);
+        R v1 = h1 ? ld(c1) : R(0);
+        while (h0) {
+            const bool h2 = h1 && gen(c2);
+            const R v2 = h2 ? ld(c2) : R(0);
+            use(c0, v0);
+            c0 = c1; v0 = v1; h0 = h1;
+            c1 = c2; v1 = v2; h1 = h2;
         }
     }
 }
@@ -261,34 +302,27 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         qq = gqlo + bit;
         return true;
     };
-    auto ld = [&](int pp, int qq) -> R { return T.FC[tri_off(qq - 2 - pp, m) + pp + 1]; };
-    int p0 = 0, q0 = 0, p1 = 0, q1 = 0, p2 = 0, q2 = 0;
-    bool h0 = gen(p0, q0);
-    R v0 = h0 ? ld(p0, q0) : R(0);
-    bool h1 = h0 && gen(p1, q1);
-    R v1 = h1 ? ld(p1, q1) : R(0);
-    while (h0) {
-        const bool h2 = h1 && gen(p2, q2);
-        const R v2 = h2 ? ld(p2, q2) : R(0);
-        if (v0 > HALF) {
-            const int l1 = p0 - i, l2 = j - q0, a = p0 + 1;
+    struct Cand { int p, q; };
+    lookahead_walk<R, Cand>(
+        [&](Cand& c) { return gen(c.p, c.q); },
+        [&](const Cand& c) -> R { return T.FC[tri_off(c.q - 2 - c.p, m) + c.p + 1]; },
+        [&](const Cand& c, R v) {
+            if (!(v > HALF)) return;
+            const int l1 = c.p - i, l2 = j - c.q, a = c.p + 1;
             R e;
             if (l1 == 0 && l2 == 0) {
                 e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
             } else {
-                const int sq = Q.s[q0], sa = Q.s[a];
-                const R jB2 = tb->jB[idx4(sq, sa, Q.s[q0 + 1], Q.s[p0])];
+                const int sq = Q.s[c.q], sa = Q.s[a];
+                const R jB2 = tb->jB[idx4(sq, sa, Q.s[c.q + 1], Q.s[c.p])];
                 R snuc = R(0);
                 if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
                 else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
                 else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
                 e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
             }
-            acc = sr.plus(acc, S::add(e, v0));
-        }
-        p0 = p1; q0 = q1; v0 = v1; h0 = h1;
-        p1 = p2; q1 = q2; v1 = v2; h1 = h2;
-    }
+            acc = sr.plus(acc, S::add(e, v));
+        });
     if (fm2 > HALF) {
         const R jA = junctionA<S>(P, L, Q, i, j);
         acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));

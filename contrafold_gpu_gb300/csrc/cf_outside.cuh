@@ -259,41 +259,36 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             enter_row();
         }
     };
-    auto ld = [&](int kind, int l1, int j) -> float {
-        if (kind == 1) return T.FM1o[tri_off(t + 2, m) + a - 1];
-        const int i = a - 1 - l1;
-        return T.FCo[tri_off(j - i, m) + i];
-    };
-    int k0 = 0, l10 = 0, j0 = 0, k1 = 0, l11 = 0, j1 = 0, k2 = 0, l12 = 0, j2 = 0;
-    bool h0 = gen(k0, l10, j0);
-    float v0 = h0 ? ld(k0, l10, j0) : 0.0f;
-    bool h1 = h0 && gen(k1, l11, j1);
-    float v1 = h1 ? ld(k1, l11, j1) : 0.0f;
-    while (h0) {
-        const bool h2 = h1 && gen(k2, l12, j2);
-        const float v2 = h2 ? ld(k2, l12, j2) : 0.0f;
-        if (k0 == 1) {
-            const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
-            acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v0, jAji), P.mp()), bp_ab));
-        } else if (v0 > CF_HALF32) {
-            const int i = a - 1 - l10, l2 = j0 - (b + 1);
-            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j0];
-            float e;
-            if (l10 == 0 && l2 == 0) {
-                e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[j0 + 1], si1, sj));
-            } else {
-                const float jBij = tb->jB[idx4(si, Q.s[j0 + 1], si1, sj)];
-                float snuc = 0.0f;
-                if (l10 == 0 && l2 == 1) snuc = P.b01(sj);
-                else if (l10 == 1 && l2 == 0) snuc = P.b01(si1);
-                else if (l10 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l10, l2), bp_ab), jBij), jB2), snuc);
+    struct Cand { int kind, l1, j; };
+    lookahead_walk<float, Cand>(
+        [&](Cand& c) { return gen(c.kind, c.l1, c.j); },
+        [&](const Cand& c) -> float {
+            if (c.kind == 1) return T.FM1o[tri_off(t + 2, m) + a - 1];
+            const int i = a - 1 - c.l1;
+            return T.FCo[tri_off(c.j - i, m) + i];
+        },
+        [&](const Cand& c, float v) {
+            if (c.kind == 1) {
+                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
+                acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v, jAji), P.mp()), bp_ab));
+                return;
             }
-            acc = sr.plus(acc, __fadd_rn(v0, e));
-        }
-        k0 = k1; l10 = l11; j0 = j1; v0 = v1; h0 = h1;
-        k1 = k2; l11 = l12; j1 = j2; v1 = v2; h1 = h2;
-    }
+            if (!(v > CF_HALF32)) return;
+            const int i = a - 1 - c.l1, l2 = c.j - (b + 1);
+            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[c.j];
+            float e;
+            if (c.l1 == 0 && l2 == 0) {
+                e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[c.j + 1], si1, sj));
+            } else {
+                const float jBij = tb->jB[idx4(si, Q.s[c.j + 1], si1, sj)];
+                float snuc = 0.0f;
+                if (c.l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                else if (c.l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                else if (c.l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(c.l1, l2), bp_ab), jBij), jB2), snuc);
+            }
+            acc = sr.plus(acc, __fadd_rn(v, e));
+        });
     T.FCo[tri_off(t, m) + a] = acc;
 }
 
@@ -347,47 +342,40 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
             gmsk = rowmask(gl1);
         }
     };
-    auto ld = [&](int kind, int l1, int j) -> float {
-        if (kind == 1) return T.FM1o[tri_off(b - a + 1, m) + a - 1];
-        const int i = a - 1 - l1;
-        return T.FCo[tri_off(j - i, m) + i];
-    };
-    int k0 = 0, l10 = 0, j0 = 0, k1 = 0, l11 = 0, j1 = 0, k2 = 0, l12 = 0, j2 = 0;
-    bool h0 = gen(k0, l10, j0);
-    float v0 = h0 ? ld(k0, l10, j0) : 0.0f;
-    bool h1 = h0 && gen(k1, l11, j1);
-    float v1 = h1 ? ld(k1, l11, j1) : 0.0f;
-    while (h0) {
-        const bool h2 = h1 && gen(k2, l12, j2);
-        const float v2 = h2 ? ld(k2, l12, j2) : 0.0f;
-        if (k0 == 1) {
-            if (v0 > CF_HALF32) {
-                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
-                const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v0, fcin), jAji), P.mp()), bp_ab), Z);
-                post = __fadd_rn(post, fexp32(pt, x));
-            }
-        } else {
-            const float outside = __fsub_rn(v0, Z);
-            if (outside > CF_HALF32) {
-                const int i = a - 1 - l10, l2 = j0 - b;
-                const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j0];
-                float e;
-                if (l10 == 0 && l2 == 0) {
-                    e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j0 + 1], si1, sj)), fcin);
-                } else {
-                    const float jBij = tb->jB[idx4(si, Q.s[j0 + 1], si1, sj)];
-                    float snuc = 0.0f;
-                    if (l10 == 0 && l2 == 1) snuc = P.b01(sj);
-                    else if (l10 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l10 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                    e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l10, l2)), fcin), bp_ab), jB2), snuc);
+    struct Cand { int kind, l1, j; };
+    lookahead_walk<float, Cand>(
+        [&](Cand& c) { return gen(c.kind, c.l1, c.j); },
+        [&](const Cand& c) -> float {
+            if (c.kind == 1) return T.FM1o[tri_off(b - a + 1, m) + a - 1];
+            const int i = a - 1 - c.l1;
+            return T.FCo[tri_off(c.j - i, m) + i];
+        },
+        [&](const Cand& c, float v) {
+            if (c.kind == 1) {
+                if (v > CF_HALF32) {
+                    const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
+                    const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, fcin), jAji), P.mp()), bp_ab), Z);
+                    post = __fadd_rn(post, fexp32(pt, x));
                 }
-                post = __fadd_rn(post, fexp32(pt, e));
+                return;
             }
-        }
-        k0 = k1; l10 = l11; j0 = j1; v0 = v1; h0 = h1;
-        k1 = k2; l11 = l12; j1 = j2; v1 = v2; h1 = h2;
-    }
+            const float outside = __fsub_rn(v, Z);
+            if (!(outside > CF_HALF32)) return;
+            const int i = a - 1 - c.l1, l2 = c.j - b;
+            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[c.j];
+            float e;
+            if (c.l1 == 0 && l2 == 0) {
+                e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[c.j + 1], si1, sj)), fcin);
+            } else {
+                const float jBij = tb->jB[idx4(si, Q.s[c.j + 1], si1, sj)];
+                float snuc = 0.0f;
+                if (c.l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                else if (c.l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                else if (c.l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(c.l1, l2)), fcin), bp_ab), jB2), snuc);
+            }
+            post = __fadd_rn(post, fexp32(pt, e));
+        });
     const float outside = __fsub_rn(T.F5o[b], Z);
     const float f5k = T.F5[a - 1];
     if (outside > CF_HALF32 && f5k > CF_HALF32) {

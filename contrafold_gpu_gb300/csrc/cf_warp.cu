@@ -13,6 +13,11 @@
 // Per-cell arithmetic is shared with the per-sequence CTA kernels
 // (cf_inside.cuh, cf_outside.cuh, cf_mea.cuh, cf_sample.cuh): results are
 // identical, bit for bit.
+// This module runs one sequence per warp: 32+ independent warps per SM hide
+// memory latency, so the chains use plain loops (no register pipelines) and a
+// small register budget keeps the SM full.
+#define CF_CHAIN_PF 0
+#define CF_WINDOW_LOOKAHEAD 0
 #include "cf_mea.cuh"
 #include "cf_outside.cuh"
 #include "cf_sample.cuh"
@@ -195,7 +200,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarpThreads, 3) k_fold_warp(WarpArgs A) {
+__global__ void __launch_bounds__(kWarpThreads, 4) k_fold_warp(WarpArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<WarpSmemHead*>(smem_raw);
     load_tabs(&sm->tabs, A.blob32);
