@@ -65,7 +65,7 @@ def main():
     args = ap.parse_args()
     from . import load
     P = load()
-    schedules = [("plain", 0), ("warp", 0), ("cta", 1), ("cta", 2), ("cta", 3), ("cta", 4)]
+    schedules = [("plain", 0), ("warp", 0), ("group", 0), ("cta", 3), ("cta", 4)]
     table = {}
     for L in [int(x) for x in args.lengths.split(",")]:
         n = int(max(304, min(20000, args.folds / L ** 3)))

@@ -105,7 +105,7 @@ namespace {
 // Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
 // Batched-path schedule by length (GB300 tuning): sequences up to this
 // length take the warp-per-sequence kernel for logZ/BPP/MEA.
-int auto_warp_max_len() { return 320; }
+int auto_warp_max_len() { return 256; }
 // CTAs per SM of the persistent CTA kernel by length.
 int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
 
@@ -119,6 +119,7 @@ int group_for_length(int L) {
 int ensure_smem(cf_engine* eng, size_t bytes);
 
 struct Plan {
+    bool plain = false;           // reference launch shape (mode 0): cf_plain.cu kernels for BPP/MEA
     bool cta = false;             // persistent CTA-per-sequence fused kernel (batched path)
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
     int wgrid = 0;                // its grid
@@ -138,6 +139,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     P.Lmax = 0;
     for (int b = 0; b < n; ++b) P.Lmax = std::max<int>(P.Lmax, (int)(offsets[b + 1] - offsets[b]));
     const bool batched = eng->mode == 1;
+    P.plain = !batched;
     if (batched) {
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
             return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
@@ -165,7 +167,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // sequences per SM in flight (their tables stay in L2); the warp kernel
     // runs one sequence per warp (short sequences, sampling).
     int sched = eng->sched;
-    if (sched == 0) sched = (job == JOB_SAMPLE || P.Lmax <= auto_warp_max_len()) ? 1 : 2;
+    if (sched == 0) sched = (job == JOB_SAMPLE || P.Lmax <= auto_warp_max_len()) ? 1 : 3;   // 3: grouped kernels
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
@@ -262,7 +264,9 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     int dev_max = 0;
     CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device));
     if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");
-    const void* ks[] = {(const void*)cf::k_inside32, (const void*)cf::k_inside32acc, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
+    const void* ks[] = {(const void*)cf::k_plain_inside32, (const void*)cf::k_plain_outside32,
+                        (const void*)cf::k_plain_posterior32, (const void*)cf::k_plain_mea32,
+                        (const void*)cf::k_inside32, (const void*)cf::k_inside32acc, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
                         (const void*)cf::k_posterior32, (const void*)cf::k_mea32, (const void*)cf::k_viterbi64};
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (int mode = 0; mode < 4; ++mode)
@@ -411,7 +415,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
     }
     const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
     const size_t smem = cf::fold_smem_bytes(P.Lmax, P.group, fp64);
-    if ((rc = ensure_smem(eng, smem))) return rc;
+    if ((rc = ensure_smem(eng, std::max(smem, cf::plain_smem_bytes(P.Lmax))))) return rc;
 
     for (size_t s = 0; s + 1 < P.slice_begin.size(); ++s) {
         const int k0 = P.slice_begin[s], k1 = P.slice_begin[s + 1];
@@ -444,6 +448,21 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
             case JOB_MEA: {
                 cf::FoldArgs Ai = A;
                 Ai.logz = nullptr;
+                if (P.plain) {
+                    const size_t psm = cf::plain_smem_bytes(P.Lmax);
+                    CF_PHASE(0, (cf::k_plain_inside32<<<grid, blk, psm, st>>>(Ai)));
+                    CF_PHASE(1, (cf::k_plain_outside32<<<grid, blk, psm, st>>>(A)));
+                    if (job == JOB_BPP) {
+                        CF_PHASE(2, (cf::k_plain_posterior32<<<grid, blk, psm, st>>>(A)));
+                    } else {
+                        cf::FoldArgs Ap = A;
+                        Ap.post_out = nullptr;
+                        Ap.logz = nullptr;
+                        CF_PHASE(2, (cf::k_plain_posterior32<<<grid, blk, psm, st>>>(Ap)));
+                        CF_PHASE(3, (cf::k_plain_mea32<<<grid, blk, psm, st>>>(A)));
+                    }
+                    break;
+                }
                 CF_PHASE(0, (cf::k_inside32<<<grid, blk, smem, st>>>(Ai)));
                 CF_PHASE(1, (cf::k_outside32<<<grid, blk, smem, st>>>(A)));
                 if (job == JOB_BPP) {
@@ -652,7 +671,7 @@ int cf_engine_set_mode(cf_engine* e, int mode) {
 
 int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
-    if (kind < 0 || kind > 2 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
+    if (kind < 0 || kind > 3 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
     e->sched = kind;
     e->ctas_per_sm = ctas_per_sm;
     return CF_OK;

@@ -40,6 +40,13 @@ __global__ void k_viterbi64(FoldArgs A);
 
 size_t fold_smem_bytes(int Lmax, int group, bool fp64);
 
+// Plain path: the reference's launch shape (cf_plain.cu), one sequence per CTA.
+__global__ void k_plain_inside32(FoldArgs A);
+__global__ void k_plain_outside32(FoldArgs A);
+__global__ void k_plain_posterior32(FoldArgs A);
+__global__ void k_plain_mea32(FoldArgs A);
+size_t plain_smem_bytes(int Lmax);
+
 // Persistent fused per-sequence kernel (one CTA per sequence at a time).
 enum { kCtaLogZ = 0, kCtaMea = 1, kCtaBpp = 2 };
 template <int MODE>

@@ -40,8 +40,9 @@ struct OutTabs {
 // F5o (cpu.py:684-699) by one warp, k = L-1 .. 0.  Target k receives, in the
 // reference's order, the pair terms of iterations j = L .. k+2 and then the
 // unpaired term F5o[k+1] + eu of iteration j = k+1.
+template <class QV>
 __device__ __forceinline__ void exterior_outside_warp(const Lse32& sr, const SmemTabs<float>* __restrict__ tb,
-                                                      const SeqV& Q, const OutTabs& T) {
+                                                      const QV& Q, const OutTabs& T) {
     const ParamView<float> P{tb->blob};
     const int L = Q.L, lane = threadIdx.x & 31;
     if (lane == 0) T.F5o[L] = 0.0f;

@@ -167,8 +167,8 @@ class Engine:
         self.mode = mode
 
     def set_schedule(self, kind: str = "auto", ctas_per_sm: int = 0):
-        """Batched-path schedule: 'auto', 'warp' or 'cta' (+ CTA residency cap)."""
-        self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2}[kind],
+        """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap) or 'group'."""
+        self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3}[kind],
                                                     int(ctas_per_sm)))
 
     def set_budget(self, nbytes: int):

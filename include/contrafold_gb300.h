@@ -85,14 +85,17 @@ int cf_engine_set_params(cf_engine* eng, const float* params32, const double* pa
  * larger than the budget are processed in slices; a single sequence that does
  * not fit returns CF_ENOMEM. */
 int cf_engine_set_budget(cf_engine* eng, size_t bytes);
-/* Select the scheduling of the FP32 fold kernels: 0 = plain (one CTA per
- * sequence, the reference's gpu.py:508 launch shape), 1 = batched (length-
- * bucketed groups, autotuned group size).  Results are identical. */
+/* Select the scheduling of the fold kernels: 0 = plain (one CTA per
+ * sequence, threads over the cells of each span, whole-window scans: the
+ * reference's gpu.py:55-184 launch shape), 1 = batched (persistent kernels
+ * and length-grouped kernels chosen per length range, see
+ * cf_engine_set_schedule).  Results are identical. */
 int cf_engine_set_mode(cf_engine* eng, int mode);
 /* Batched-path schedule (the tuner's knob): kind 0 = automatic by length,
  * 1 = persistent warp-per-sequence kernel, 2 = persistent CTA-per-sequence
- * fused kernel; ctas_per_sm caps the CTA kernel's residency (0 = automatic).
- * Results are identical for every choice. */
+ * fused kernel, 3 = length-grouped per-phase kernels; ctas_per_sm caps the
+ * persistent CTA kernel's residency (0 = automatic).  Results are identical
+ * for every choice. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
 
 const char* cf_last_error(void);

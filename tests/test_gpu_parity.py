@@ -18,7 +18,7 @@ from conftest import golden_post, mask_of
 pytestmark = pytest.mark.gpu
 
 
-PATHS = ["plain", "warp", "cta"]
+PATHS = ["plain", "warp", "cta", "group"]
 
 
 def set_path(engine, path):
@@ -147,7 +147,7 @@ def test_plain_equals_batched(engine):
         res[path] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B), z, np.concatenate([m.ravel() for m in mats]))
     set_path(engine, "cta")
     engine.set_schedule("auto")
-    for path in ("warp", "cta"):
+    for path in ("warp", "cta", "group"):
         assert np.array_equal(res["plain"][0], res[path][0])
         assert res["plain"][1] == res[path][1]
         assert res["plain"][2] == res[path][2]
