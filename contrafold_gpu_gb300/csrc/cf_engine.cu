@@ -63,7 +63,7 @@ struct DevBuf {
     }
 };
 
-enum Job { JOB_LOGZ = 0, JOB_LOGZ64, JOB_BPP, JOB_MEA, JOB_MFE, JOB_SAMPLE };
+enum Job { JOB_LOGZ = 0, JOB_LOGZ64, JOB_BPP, JOB_MEA, JOB_MFE, JOB_SAMPLE, JOB_GRAD };
 
 int64_t arena_words(Job job, int L) {
     switch (job) {
@@ -71,6 +71,7 @@ int64_t arena_words(Job job, int L) {
         case JOB_SAMPLE: return cf::pad32(cf::arena32_inside_words(L));
         case JOB_LOGZ64:
         case JOB_MFE: return cf::arena64(L).total;
+        case JOB_GRAD: return cf::pad32(cf::adj_arena_words(L));
         default: return cf::arena32(L).total;
     }
 }
@@ -92,6 +93,8 @@ struct cf_engine {
     DevBuf<int64_t> post_offs;
     DevBuf<int> status;
     DevBuf<char> samples;
+    DevBuf<float> bonus;
+    DevBuf<double> counts, unpaired;
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
     int mode = 1;        // 0 plain, 1 batched
     int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent
@@ -138,7 +141,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     P.group = 1;
     P.Lmax = 0;
     for (int b = 0; b < n; ++b) P.Lmax = std::max<int>(P.Lmax, (int)(offsets[b + 1] - offsets[b]));
-    const bool batched = eng->mode == 1;
+    const bool batched = eng->mode == 1 && job != JOB_GRAD;
     P.plain = !batched;
     if (batched) {
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
@@ -638,6 +641,7 @@ int cf_engine_destroy(cf_engine* e) {
     e->blob32.release(); e->blob64.release(); e->arena.release(); e->seqs.release(); e->mask.release();
     e->descs.release(); e->logz.release(); e->logz64.release(); e->structs.release(); e->post.release();
     e->post_offs.release(); e->status.release(); e->samples.release();
+    e->bonus.release(); e->counts.release(); e->unpaired.release();
 
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -717,6 +721,71 @@ int cf_sample(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const u
 }
 
 }  // extern "C"
+
+// ============================ adjoint ============================
+extern "C" int cf_grad(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+                       const float* bonus, float* logz_out, double* counts_out, double* unpaired_out) {
+    int rc = check_batch(e, seqs, offsets, n);
+    if (rc) return rc;
+    if (n > 0 && (!counts_out || !unpaired_out)) return fail(CF_EINVAL, "counts_out / unpaired_out is NULL");
+    if (n == 0) return CF_OK;
+    CF_CUDA(cudaSetDevice(e->device));
+    cudaStream_t st = e->stream;
+    Plan P;
+    if ((rc = make_plan(e, JOB_GRAD, offsets, n, P))) return rc;
+    const size_t nbytes = (size_t)offsets[n];
+    if ((rc = e->seqs.ensure(std::max<size_t>(nbytes, 1)))) return rc;
+    if (nbytes) CF_CUDA(cudaMemcpyAsync(e->seqs.p, seqs, nbytes, cudaMemcpyHostToDevice, st));
+    const uint8_t* d_mask = nullptr;
+    if (mask) {
+        if ((rc = e->mask.ensure(std::max<size_t>(nbytes, 1)))) return rc;
+        if (nbytes) CF_CUDA(cudaMemcpyAsync(e->mask.p, mask, nbytes, cudaMemcpyHostToDevice, st));
+        d_mask = e->mask.p;
+    }
+    const float* d_bonus = nullptr;
+    if (bonus) {
+        if ((rc = e->bonus.ensure(std::max<size_t>(nbytes, 1)))) return rc;
+        if (nbytes) CF_CUDA(cudaMemcpyAsync(e->bonus.p, bonus, nbytes * sizeof(float), cudaMemcpyHostToDevice, st));
+        d_bonus = e->bonus.p;
+    }
+    if ((rc = e->counts.ensure((size_t)n * CF_BLOB_LEN)) || (rc = e->unpaired.ensure(std::max<size_t>(nbytes, 1))) ||
+        (rc = e->logz.ensure(n)) || (rc = e->descs.ensure(n)) || (rc = e->status.ensure(2)))
+        return rc;
+    CF_CUDA(cudaMemcpyAsync(e->descs.p, P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice, st));
+    CF_CUDA(cudaMemsetAsync(e->status.p, 0, sizeof(int), st));
+    int64_t maxw = 1;
+    for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
+    if ((rc = e->arena.ensure((size_t)maxw))) return rc;
+    const size_t smem = cf::adj_smem_bytes(P.Lmax);
+    if (smem > 48 * 1024 - CF_BLOB_LEN * 8) return fail(CF_EINVAL, "sequence too long for the adjoint kernels");
+    for (size_t sl = 0; sl + 1 < P.slice_begin.size(); ++sl) {
+        const int k0 = P.slice_begin[sl], k1 = P.slice_begin[sl + 1];
+        cf::FoldArgs A;
+        A.descs = e->descs.p + k0;
+        A.n = k1 - k0;
+        A.group = 1;
+        A.seqs = e->seqs.p;
+        A.mask = d_mask;
+        A.blob32 = e->blob32.p;
+        A.blob64 = e->blob64.p;
+        A.ws = e->arena.p;
+        A.logz = e->logz.p;
+        A.logz64 = nullptr;
+        A.structs = nullptr;
+        A.post_out = nullptr;
+        A.post_offs = nullptr;
+        A.gamma = 0.f;
+        A.status = e->status.p;
+        cf::k_adj_inside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus);
+        cf::k_adj_outside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus);
+        cf::k_adj_counts<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus, e->counts.p, e->unpaired.p);
+        CF_CUDA(cudaGetLastError());
+    }
+    CF_CUDA(cudaMemcpyAsync(counts_out, e->counts.p, sizeof(double) * n * CF_BLOB_LEN, cudaMemcpyDeviceToHost, st));
+    if (nbytes) CF_CUDA(cudaMemcpyAsync(unpaired_out, e->unpaired.p, sizeof(double) * nbytes, cudaMemcpyDeviceToHost, st));
+    if (logz_out) CF_CUDA(cudaMemcpyAsync(logz_out, e->logz.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+    return read_status(e, st);
+}
 
 // ============================ plans (device-resident batches) ============================
 struct cf_plan {

@@ -25,7 +25,7 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
            "cf_engine_set_mode", "cf_engine_set_schedule", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
-           "cf_mea", "cf_mfe", "cf_sample", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
+           "cf_mea", "cf_mfe", "cf_sample", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group")
 CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE = 0, 1, 3, 4

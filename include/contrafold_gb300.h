@@ -138,6 +138,20 @@ int cf_sample(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
               const uint8_t* mask, int32_t n, int32_t n_samples, uint64_t seed,
               char* out);
 
+/* Differentiation of logZ (no reference counterpart: the reference has no
+ * gradient).  With an optional soft per-position unpaired bonus `bonus`
+ * (float32, laid out like `seqs`; NULL = 0) added to the score of every
+ * unpaired position, returns per sequence b:
+ *   logz_out[b]                          logZ (accurate float32 log-sum-exp)
+ *   counts_out[b*CF_BLOB_LEN + e]        d logZ / d(parameter-blob entry e) =
+ *                                        expected uses of entry e (FP64 sums)
+ *   unpaired_out[offsets[b] + t]         d logZ / d bonus_t = P(t unpaired)
+ * The raw-feature gradient is counts_out times the tying Jacobian of the
+ * loader (linear, gpu_contrafold/cpu.py:40-135). */
+int cf_grad(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+            const uint8_t* mask, int32_t n, const float* bonus, float* logz_out,
+            double* counts_out, double* unpaired_out);
+
 /* ---- plans: device-resident batches ----
  * A plan fixes a batch's shape (lengths from host `offsets`), orders and
  * groups its sequences, and owns the device descriptors and a work arena sized

@@ -166,6 +166,105 @@ double oracle_inside64(const int8_t* s, int L, const int8_t* forced, const doubl
     return z;
 }
 
+/* Extension of inside64 (not in the reference): a soft per-position unpaired
+ * bonus u[1..L] added for every unpaired position -- hairpin interiors,
+ * single-branch loop interiors, multiloop (FM1 / FM extensions) and exterior
+ * unpaired positions.  With u == NULL this is inside64.  Used as the FP64
+ * finite-difference oracle of the adjoint. */
+double oracle_inside64_bonus(const int8_t* s, int L, const int8_t* forced, const double* blob,
+                             const double* u) {
+    if (!u) return oracle_inside64(s, L, forced, blob, NULL);
+    P64 P = unpack64(blob);
+    const int n = L + 2;
+    double* U = (double*)calloc((size_t)n, sizeof(double));
+    for (int k = 1; k <= L; ++k) U[k] = U[k - 1] + u[k];
+    double* FC = (double*)malloc(sizeof(double) * (3 * (size_t)n * n + n));
+    double* FM = FC + (size_t)n * n;
+    double* FM1 = FM + (size_t)n * n;
+    double* F5 = FM1 + (size_t)n * n;
+    for (size_t t = 0; t < 3 * (size_t)n * n + n; ++t) FC[t] = NEG64;
+    for (int i = L; i >= 0; --i) {
+        for (int j = i; j <= L; ++j) {
+            double FM2 = NEG64;
+            for (int k = i + 1; k < j; ++k)
+                if (T(FM1, i, k) > HALF64 && T(FM, k, j) > HALF64)
+                    FM2 = lse64(FM2, T(FM1, i, k) + T(FM, k, j));
+            if (0 < i && j < L && OK_PAIR(i, j + 1)) {
+                double sum = NEG64;
+                double jB = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
+                sum = lse64(sum, jB + P.hp[j - i <= DHP ? j - i : DHP] + (U[j] - U[i]));
+                int pmax = i + CMAX < j ? i + CMAX : j;
+                for (int p = i; p <= pmax; ++p) {
+                    int l1 = p - i;
+                    int qmin = p + 2, alt = p - i + j - CMAX;
+                    if (alt > qmin) qmin = alt;
+                    for (int q = j; q >= qmin; --q) {
+                        int l2 = j - q;
+                        if (OK_PAIR(p + 1, q) && T(FC, p + 1, q - 1) > HALF64) {
+                            double e;
+                            if (p == i && q == j) {
+                                e = P.bp[I2(s[i + 1], s[j])] + P.stack[I4(s[i], s[j + 1], s[i + 1], s[j])];
+                            } else {
+                                double jB1 = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
+                                double jB2 = P.hc[I2(s[q], s[p + 1])] + P.tm[I4(s[q], s[p + 1], s[q + 1], s[p])];
+                                double snuc = 0.0;
+                                if (l1 == 0 && l2 == 1) snuc = P.b01[s[j]];
+                                else if (l1 == 1 && l2 == 0) snuc = P.b01[s[i + 1]];
+                                else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
+                                e = P.cs[l1 * 31 + l2] + P.bp[I2(s[p + 1], s[q])] + jB1 + jB2 + snuc;
+                            }
+                            double bon = (U[p] - U[i]) + (U[j] - U[q]);
+                            sum = lse64(sum, e + T(FC, p + 1, q - 1) + bon);
+                        }
+                    }
+                }
+                if (FM2 > HALF64) {
+                    double jA = P.hc[I2(s[i], s[j + 1])];
+                    if (i < L) jA += P.dl[I3(s[i], s[j + 1], s[i + 1])];
+                    if (j > 0) jA += P.dr[I3(s[i], s[j + 1], s[j])];
+                    sum = lse64(sum, FM2 + jA + P.mp + P.mb);
+                }
+                T(FC, i, j) = sum;
+            }
+            if (0 < i && i + 2 <= j && j < L) {
+                double sum = NEG64;
+                if (OK_PAIR(i + 1, j) && T(FC, i + 1, j - 1) > HALF64) {
+                    double jAji = P.hc[I2(s[j], s[i + 1])];
+                    if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
+                    if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
+                    sum = lse64(sum, T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
+                }
+                if (T(FM1, i + 1, j) > HALF64) sum = lse64(sum, T(FM1, i + 1, j) + P.mu + u[i + 1]);
+                T(FM1, i, j) = sum;
+            }
+            if (0 < i && i + 2 <= j && j < L) {
+                double sum = NEG64;
+                if (FM2 > HALF64) sum = lse64(sum, FM2);
+                if (T(FM, i, j - 1) > HALF64) sum = lse64(sum, T(FM, i, j - 1) + P.mu + u[j]);
+                if (T(FM1, i, j) > HALF64) sum = lse64(sum, T(FM1, i, j));
+                T(FM, i, j) = sum;
+            }
+        }
+    }
+    F5[0] = 0.0;
+    for (int j = 1; j <= L; ++j) {
+        double sum = F5[j - 1] + P.eu + u[j];
+        for (int k = 0; k < j; ++k) {
+            if (OK_PAIR(k + 1, j) && T(FC, k + 1, j - 1) > HALF64 && F5[k] > HALF64) {
+                double jA = P.hc[I2(s[j], s[k + 1])];
+                if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
+                if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
+                sum = lse64(sum, F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
+            }
+        }
+        F5[j] = sum;
+    }
+    double z = F5[L];
+    free(FC);
+    free(U);
+    return z;
+}
+
 /* Viterbi + EPS first-match traceback (cpu.py:290-502).  pair[0..L+1]
  * receives the 1-based partner of each position or -1. */
 void oracle_viterbi64(const int8_t* s, int L, const int8_t* forced, const double* blob,

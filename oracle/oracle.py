@@ -55,6 +55,8 @@ def lib():
         L.oracle_lse32.argtypes = [ctypes.c_float, ctypes.c_float]
         L.oracle_fexp32.restype = ctypes.c_float
         L.oracle_fexp32.argtypes = [ctypes.c_float]
+        L.oracle_inside64_bonus.restype = ctypes.c_double
+        L.oracle_inside64_bonus.argtypes = [i8p, ctypes.c_int, i8p, f64p, f64p]
         L.oracle_count_mea_ops.restype = None
         L.oracle_count_mea_ops.argtypes = [i8p, ctypes.c_int, i8p, f32p, ctypes.c_float, i64p]
         u8p = P(ctypes.c_uint8)
@@ -98,6 +100,20 @@ def logz64(seq, P, forced=None) -> float:
     _, b64 = _blobs(P)
     return float(lib().oracle_inside64(_ptr(s, ctypes.c_int8), L, _ptr(fo, ctypes.c_int8),
                                        _ptr(b64, ctypes.c_double), None))
+
+
+def logz64_bonus(seq, P, bonus=None, forced=None, blob64=None) -> float:
+    """FP64 logZ with a per-position unpaired bonus (our extension of cpu.py:165-275;
+    the reference has no bonus).  `blob64` overrides the parameter blob."""
+    s, fo, L = encode(seq, forced)
+    b64 = blob64 if blob64 is not None else _blobs(P)[1]
+    u = None
+    if bonus is not None:
+        u = np.zeros(L + 2, np.float64)
+        u[1:L + 1] = np.asarray(bonus, np.float64)[:L]
+    return float(lib().oracle_inside64_bonus(_ptr(s, ctypes.c_int8), L, _ptr(fo, ctypes.c_int8),
+                                             _ptr(np.ascontiguousarray(b64, np.float64), ctypes.c_double),
+                                             _ptr(u, ctypes.c_double) if u is not None else None))
 
 
 def inside64_tables(seq, P, forced=None):
