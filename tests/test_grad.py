@@ -91,7 +91,8 @@ def test_grad_posterior_identities(engine, P, oracle):
         M = mats[b].astype(np.float64)
         punp = 1.0 - M.sum(0) - M.sum(1)
         assert np.max(np.abs(res.d_bonus[b] - punp)) < 1.5e-2
-        assert abs(res.d_bonus[b].sum() - (len(s) - 2 * sum(res.d_blob[b, o:o + 25]))) < 1e-6 * len(s)
+        # every position is paired or unpaired: sum_k P(unpaired) = L - 2 E[#pairs] (float32 tables)
+        assert abs(res.d_bonus[b].sum() - (len(s) - 2 * sum(res.d_blob[b, o:o + 25]))) < 1e-4 * len(s)
         code = [params.CODE.get(c, 4) for c in s]
         for (x, y), fname in feat.items():
             got = res.d_blob[b, o + x * 5 + y] + res.d_blob[b, o + y * 5 + x]
