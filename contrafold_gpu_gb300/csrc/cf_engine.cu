@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/contrafold_gb300.h"
+#include "cf_host.h"
 #include "cf_kernels.h"
 #include "cf_sample.h"
 #include "cf_warp.h"
@@ -886,3 +887,14 @@ int cf_plan_launches(const cf_plan* p) { return p ? p->launches : 0; }
 int cf_plan_group(const cf_plan* p) { return p ? p->P.group : 0; }
 
 }  // extern "C"
+
+// ============================ accessors for other host units (cf_host.h) ============================
+namespace cf {
+
+int engine_device(const cf_engine* e) { return e->device; }
+cudaStream_t engine_stream(const cf_engine* e) { return e->stream; }
+const float* engine_blob32(const cf_engine* e) { return e->blob32.p; }
+int engine_ensure_smem(cf_engine* e, size_t bytes) { return ensure_smem(e, bytes); }
+int engine_fail(int code, const char* msg) { return fail(code, msg); }
+
+}  // namespace cf

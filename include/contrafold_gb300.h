@@ -183,6 +183,27 @@ int cf_plan_phase_ms(cf_plan* plan, float* ms, int32_t nphases);
 int cf_plan_launches(const cf_plan* plan);
 int cf_plan_group(const cf_plan* plan);
 
+/* ---- MEA without device allocation ----
+ * No reference counterpart: the reference allocates its device buffers with
+ * Numba on every call.  Same arguments, results and argument errors as cf_mea,
+ * but the call allocates no device memory: inputs, descriptors, outputs and the
+ * fold arenas live in one static device array of CF_SCRATCH_BYTES, reserved by
+ * the driver when the library's module is loaded.  For callers that cannot let
+ * a library allocate while they run (a framework allocator has reserved the
+ * device; cudaFree would stall a serving loop's other streams).
+ * - Batches whose inputs, outputs and 8 fold slots for the longest sequence do
+ *   not fit (longest sequence above ~740 nt, or too many nucleotides) are
+ *   rejected with CF_EINVAL and a message giving the bytes needed.
+ * - The first call on a device does set-up (resolves the array's address);
+ *   make it before any stream capture begins.
+ * - The status word and work-queue head must be zero at launch: the call
+ *   clears them itself.  Calls share the array, so overlapping calls would
+ *   race; the library serialises them with a process-wide lock and each call
+ *   returns only after its work has finished.  Synchronous, engine's stream. */
+#define CF_SCRATCH_BYTES (64u * 1024u * 1024u)
+int cf_mea_scratch(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+                   const uint8_t* mask, int32_t n, float gamma, char* struct_out);
+
 #ifdef __cplusplus
 }
 #endif
