@@ -381,6 +381,77 @@ def our_arm(args):
     return 0
 
 
+def serving_arm(args):
+    """Open-loop serving sweep: saturated throughput (every request queued at
+    t = 0), then Poisson streams at fractions of it; p50 / p99 latency from the
+    scheduled arrival to the result, per offered load.  Requests: log-normal
+    lengths (median 150 nt, log-sd 0.6, clipped to 30-1000), 40 % logZ / 40 %
+    MEA (gamma 6) / 20 % ten Boltzmann samples, 10 % carrying a Bernoulli(0.1)
+    forced-unpaired mask.  A sample of results is compared with the same
+    requests folded alone."""
+    from contrafold_gpu_gb300 import load, serve
+    from contrafold_gpu_gb300.engine import Batch, Engine
+    P = load()
+    out = {"metric": "serving p99 latency at 80% of saturated throughput", "unit": "ms",
+           "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+           "config": {"workload": "serving: Poisson arrivals, lengths log-normal median 150 nt sigma 0.6 clipped 30-1000, "
+                                  "40% logZ / 40% MEA / 20% sample x10, 10% masked",
+                      "workers": args.workers, "long_workers": args.long_workers}}
+    with serve.Server(P, workers=args.workers, long_workers=args.long_workers) as srv:
+        warm, _ = serve.mixed_workload(2000, rate=1e9, seed=99)
+        srv.replay(warm, np.zeros(len(warm)), keep_results=False)
+        n_sat = args.serve_n
+        reqs, _ = serve.mixed_workload(n_sat, rate=1e9, seed=100)
+        with ClockSampler(0) as clk:
+            rep = srv.replay(reqs, np.zeros(n_sat), keep_results=False)
+            sat = n_sat / (rep.latency_ms.max() / 1e3)
+            points = []
+            check_frac = min(args.serve_fracs, key=lambda f: abs(f - 0.8))
+            for frac in args.serve_fracs:
+                rate = frac * sat
+                n = max(500, int(rate * args.serve_seconds))
+                reqs, t = serve.mixed_workload(n, rate=rate, seed=int(frac * 1000))
+                st0 = srv.stats()
+                rep = srv.replay(reqs, t, keep_results=(frac == check_frac))
+                st1 = srv.stats()
+                lat = rep.latency_ms
+                pt = {"offered_frac": frac, "offered_rps": round(rate, 1),
+                      "achieved_rps": round(n / float(np.max(t + lat / 1e3)), 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                      "max_ms": round(float(lat.max()), 3),
+                      "mean_batch": round((st1["done"] - st0["done"]) / max(1, st1["batches"] - st0["batches"]), 1),
+                      "errors": int(np.count_nonzero(rep.status))}
+                for op in ("logz", "mea", "sample"):
+                    sel = np.array([r.op == op for r in reqs])
+                    pt[f"p99_{op}_ms"] = round(float(np.percentile(lat[sel], 99)), 3)
+                points.append(pt)
+                if frac == check_frac:
+                    check = (reqs, rep.results)
+        clocks = clk.summary()
+    # same-as-alone check on a seeded sample of the 80 % run
+    eng = Engine(P)
+    reqs, results = check
+    idx = np.random.default_rng(0).choice(len(reqs), min(200, len(reqs)), replace=False)
+    bad = 0
+    for k in idx:
+        r = reqs[k]
+        B = Batch([r.seq], None if r.mask is None else [r.mask])
+        if r.op == "logz":
+            ok = abs(float(eng.logz(B)[0]) - results[k]) <= 1e-5 * max(1.0, abs(results[k]))
+        elif r.op == "mea":
+            ok = eng.mea(B, r.gamma)[0] == results[k]
+        else:
+            ok = eng.sample(B, r.n_samples, seed=r.seed)[0] == results[k]
+        bad += 0 if ok else 1
+    eng.close()
+    p80 = next(p for p in points if p["offered_frac"] == check_frac)
+    out.update({"value": p80["p99_ms"], "saturated_folds_per_s": round(sat, 1), "points": points,
+                "alone_check": {"sampled": int(len(idx)), "mismatches": bad}, "clocks": clocks})
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,7 +460,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10000)
     ap.add_argument("--L", type=int, default=200)
+    ap.add_argument("--workload", choices=["mea", "serving"], default="mea",
+                    help="mea: the headline 200-nt MEA batch; serving: the open-loop request-stream sweep")
+    ap.add_argument("--workers", type=int, default=6, help="serving: engines / worker threads")
+    ap.add_argument("--long-workers", type=int, default=2, help="serving: workers that take long requests")
+    ap.add_argument("--serve-n", type=int, default=20000, help="serving: requests of the saturation run")
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: seconds of arrivals per load point")
+    ap.add_argument("--serve-fracs", type=float, nargs="+", default=[0.2, 0.5, 0.8, 0.9])
     args = ap.parse_args()
+    if args.workload == "serving":
+        return serving_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return our_arm(args)

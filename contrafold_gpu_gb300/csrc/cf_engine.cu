@@ -94,6 +94,7 @@ struct cf_engine {
     DevBuf<int64_t> post_offs;
     DevBuf<int> status;
     DevBuf<char> samples;
+    DevBuf<uint64_t> seeds;
     DevBuf<float> bonus;
     DevBuf<double> counts, unpaired;
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
@@ -107,9 +108,13 @@ namespace {
 
 // ---- group-size autotune table: sequences per CTA by length range ----
 // Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
-// Batched-path schedule by length (GB300 tuning): sequences up to this
-// length take the warp-per-sequence kernel for logZ/BPP/MEA.
+// Batched-path schedule (GB300 tuning): batches of at least
+// auto_warp_min_batch() sequences, none longer than auto_warp_max_len(), take
+// the warp-per-sequence kernel (throughput); smaller batches fold one sequence
+// per CTA (latency: a single 250-nt MEA fold takes 56 ms on a CTA, 232 ms on a
+// warp).
 int auto_warp_max_len() { return 256; }
+int auto_warp_min_batch() { return 1024; }
 // CTAs per SM of the persistent CTA kernel by length.
 int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
 
@@ -148,9 +153,13 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
             return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
         });
-        // one group size for the launch: that of the median length
+        // one group size for the launch: that of the median length, but only as
+        // many sequences per CTA as still leave two CTAs per SM
         const int Lmed = n ? (int)(offsets[order[n / 2] + 1] - offsets[order[n / 2]]) : 0;
-        P.group = std::min(cf::kMaxGroup, group_for_length(Lmed));
+        int sms = 0;
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        const int fill = std::max(1, n / std::max(1, 2 * sms));
+        P.group = std::min(std::min(cf::kMaxGroup, group_for_length(Lmed)), fill);
     }
     for (int k = 0; k < n; ++k) {
         const int b = order[k];
@@ -171,7 +180,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // sequences per SM in flight (their tables stay in L2); the warp kernel
     // runs one sequence per warp (short sequences, sampling).
     int sched = eng->sched;
-    if (sched == 0) sched = (job == JOB_SAMPLE || P.Lmax <= auto_warp_max_len()) ? 1 : 3;   // 3: grouped kernels
+    if (sched == 0) sched = (P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch()) ? 1 : 3;   // 3: grouped
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
@@ -329,6 +338,7 @@ struct PhaseTimer {
 struct SampleJob {
     int n_samples = 0;
     uint64_t seed = 0;
+    const uint64_t* d_seeds = nullptr;   // per-sequence seeds (cf_sample_seeded) or null
     char* d_out = nullptr;
 };
 
@@ -406,6 +416,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         W.post_offs = d_post_offs;
         W.n_samples = sj ? sj->n_samples : 0;
         W.seed = sj ? sj->seed : 0;
+        W.seeds = sj ? sj->d_seeds : nullptr;
         W.out = sj ? sj->d_out : nullptr;
         W.status = X.status;
         const int mode = job == JOB_LOGZ ? cf::kWarpLogZ : job == JOB_MEA ? cf::kWarpMea
@@ -492,6 +503,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                 S.n_samples = sj->n_samples;
                 S.Lmax = P.Lmax;
                 S.seed = sj->seed;
+                S.seeds = sj->d_seeds;
                 S.seqs = d_seqs;
                 S.mask = d_mask;
                 S.blob32 = eng->blob32.p;
@@ -527,7 +539,7 @@ int read_status(cf_engine* eng, cudaStream_t st) {
 int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask,
              int32_t n, float gamma, float* logz_out, double* logz64_out, char* struct_out,
              const int64_t* post_offsets, float* post_out, int n_samples = 0, uint64_t seed = 0,
-             char* sample_out = nullptr) {
+             char* sample_out = nullptr, const uint64_t* seeds = nullptr) {
     int rc = check_batch(eng, seqs, offsets, n);
     if (rc) return rc;
     if (n == 0) return CF_OK;
@@ -581,6 +593,11 @@ int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offset
         sj.n_samples = n_samples;
         sj.seed = seed;
         sj.d_out = eng->samples.p;
+        if (seeds) {
+            if ((rc = eng->seeds.ensure(n))) return rc;
+            CF_CUDA(cudaMemcpyAsync(eng->seeds.p, seeds, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+            sj.d_seeds = eng->seeds.p;
+        }
     }
     if ((rc = eng->descs.ensure(n))) return rc;
     CF_CUDA(cudaMemcpyAsync(eng->descs.p, P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice, st));
@@ -641,7 +658,7 @@ int cf_engine_destroy(cf_engine* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->blob32.release(); e->blob64.release(); e->arena.release(); e->seqs.release(); e->mask.release();
     e->descs.release(); e->logz.release(); e->logz64.release(); e->structs.release(); e->post.release();
-    e->post_offs.release(); e->status.release(); e->samples.release();
+    e->post_offs.release(); e->status.release(); e->samples.release(); e->seeds.release();
     e->bonus.release(); e->counts.release(); e->unpaired.release();
 
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -719,6 +736,14 @@ int cf_sample(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const u
     if (n > 0 && n_samples > 0 && !out) return fail(CF_EINVAL, "out is NULL");
     return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, n_samples,
                     seed, out);
+}
+
+int cf_sample_seeded(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+                     int32_t n_samples, const uint64_t* seeds, char* out) {
+    if (n_samples < 0) return fail(CF_EINVAL, "n_samples must be >= 0");
+    if (n > 0 && n_samples > 0 && (!out || !seeds)) return fail(CF_EINVAL, "out / seeds is NULL");
+    return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, n_samples,
+                    0, out, seeds);
 }
 
 }  // extern "C"

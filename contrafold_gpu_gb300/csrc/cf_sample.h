@@ -14,6 +14,8 @@ struct SampleArgs {
     int n_samples;
     int Lmax;
     uint64_t seed;
+    const uint64_t* seeds;  // null, or one seed per batch index: sequence b then samples with key
+                            // seeds[b] and sequence index 0, exactly as if it were folded alone
     const uint8_t* seqs;
     const uint8_t* mask;
     const float* blob32;

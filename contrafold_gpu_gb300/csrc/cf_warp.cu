@@ -122,12 +122,14 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
         X.tb = &sm->tabs;
         X.Q = Q;
         X.T = T;
-        const uint2 key = make_uint2((uint32_t)A.seed, (uint32_t)(A.seed >> 32));
+        const uint64_t sd = A.seeds != nullptr ? A.seeds[D.idx] : A.seed;
+        const uint2 key = make_uint2((uint32_t)sd, (uint32_t)(sd >> 32));
+        const int sidx = A.seeds != nullptr ? 0 : D.idx;
         for (int smp = 0; smp < A.n_samples; ++smp) {
             char* out = A.out + D.seq_off * (int64_t)A.n_samples + (int64_t)smp * L;
             for (int t = lane; t < L; t += 32) out[t] = '.';
             __syncwarp();
-            sample_one(X, smp, D.idx, key, out, stack, A.status, lane);
+            sample_one(X, smp, sidx, key, out, stack, A.status, lane);
             __syncwarp();
         }
         if (A.logz != nullptr && lane == 0) A.logz[D.idx] = T.F5[L];

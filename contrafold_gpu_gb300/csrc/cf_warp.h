@@ -30,6 +30,7 @@ struct WarpArgs {
     const int64_t* post_offs;
     int n_samples;
     uint64_t seed;
+    const uint64_t* seeds;     // null, or per batch index (see SampleArgs::seeds)
     char* out;                 // samples at seq_off * n_samples
     int* status;
 };

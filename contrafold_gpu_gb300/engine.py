@@ -17,17 +17,18 @@ from . import params as _params
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcontrafold_gb300.so")
 
-CF_OK, CF_EINVAL, CF_ENOMEM, CF_ETIMEOUT, CF_ECUDA, CF_EDEVICE = 0, 1, 2, 3, 4, 5
+CF_OK, CF_EINVAL, CF_ENOMEM, CF_ETIMEOUT, CF_ECUDA, CF_EDEVICE, CF_ECANCELLED = 0, 1, 2, 3, 4, 5, 6
 CF_MAX_LEN = 32767
 _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "device wait timed out",
-           4: "CUDA error", 5: "device-side limit"}
+           4: "CUDA error", 5: "device-side limit", 6: "cancelled"}
 
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
            "cf_engine_set_mode", "cf_engine_set_schedule", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
-           "cf_mea", "cf_mfe", "cf_sample", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
+           "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
-           "cf_plan_group")
+           "cf_plan_group", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
+           "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats")
 CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE = 0, 1, 3, 4
 
 
@@ -68,6 +69,8 @@ def load_library(path: str = LIB_PATH):
         L.cf_mfe.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_char_p]
         L.cf_sample.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
                                 ctypes.c_char_p]
+        L.cf_sample_seeded.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, P(ctypes.c_uint64),
+                                       ctypes.c_char_p]
         L.cf_plan_create.argtypes = [vp, ctypes.c_int32, i64p, ctypes.c_int32, P(vp)]
         L.cf_plan_destroy.argtypes = [vp]
         L.cf_plan_arena_bytes.argtypes = [vp]
@@ -80,7 +83,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_group.argtypes = [vp]
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
                      "cf_engine_set_mode", "cf_engine_set_schedule", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
-                     "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
+                     "cf_sample_seeded", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group"):
             getattr(L, name).restype = ctypes.c_int
         _lib = L
@@ -216,13 +219,22 @@ class Engine:
             self._check(self.lib.cf_mfe(*self._args(B), out))
         return B.split_strings(out.raw[:B.total])
 
-    def sample(self, B: Batch, n_samples: int, seed: int = 0) -> List[List[str]]:
+    def sample(self, B: Batch, n_samples: int, seed: int = 0, seeds: Optional[Sequence[int]] = None) -> List[List[str]]:
+        """Samples per sequence.  With `seeds` (one per sequence) sequence b draws
+        what it draws alone with seed seeds[b] (cf_sample_seeded)."""
         if n_samples < 0:
             raise ValueError("n_samples must be >= 0")
         out = ctypes.create_string_buffer(max(B.total * n_samples, 1))
         with self._lock:
-            self._check(self.lib.cf_sample(*self._args(B), ctypes.c_int32(n_samples),
-                                           ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
+            if seeds is None:
+                self._check(self.lib.cf_sample(*self._args(B), ctypes.c_int32(n_samples),
+                                               ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
+            else:
+                sd = np.array([int(x) & 0xFFFFFFFFFFFFFFFF for x in seeds], np.uint64)
+                if sd.size != B.n:
+                    raise ValueError("one seed per sequence is required")
+                self._check(self.lib.cf_sample_seeded(*self._args(B), ctypes.c_int32(n_samples),
+                                                      _p(sd, ctypes.c_uint64), out))
         raw = out.raw[:B.total * n_samples].decode("ascii")
         res = []
         for b in range(B.n):

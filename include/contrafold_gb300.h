@@ -93,7 +93,8 @@ int cf_engine_set_budget(cf_engine* eng, size_t bytes);
 int cf_engine_set_mode(cf_engine* eng, int mode);
 /* Batched-path schedule (the tuner's knob): kind 0 = automatic by length,
  * 1 = persistent warp-per-sequence kernel, 2 = persistent CTA-per-sequence
- * fused kernel, 3 = length-grouped per-phase kernels; ctas_per_sm caps the
+ * fused kernel, 3 = length-grouped per-phase kernels (kind 0 takes the warp
+ * kernel for batches of >= 1024 sequences of <= 256 nt, else kind 3); ctas_per_sm caps the
  * persistent CTA kernel's residency (0 = automatic).  Results are identical
  * for every choice. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
@@ -137,6 +138,13 @@ int cf_mfe(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
 int cf_sample(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
               const uint8_t* mask, int32_t n, int32_t n_samples, uint64_t seed,
               char* out);
+
+/* cf_sample with one seed per sequence (no reference counterpart; the serving
+ * loop uses it): sequence b draws exactly the samples that cf_sample gives for
+ * it alone (n = 1) with seed seeds[b], whatever batch it is folded in. */
+int cf_sample_seeded(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
+                     const uint8_t* mask, int32_t n, int32_t n_samples,
+                     const uint64_t* seeds, char* out);
 
 /* Differentiation of logZ (no reference counterpart: the reference has no
  * gradient).  With an optional soft per-position unpaired bonus `bonus`
@@ -182,6 +190,66 @@ int cf_plan_phase_ms(cf_plan* plan, float* ms, int32_t nphases);
 /* Kernels launched by the last cf_plan_run; sequences per CTA of the plan. */
 int cf_plan_launches(const cf_plan* plan);
 int cf_plan_group(const cf_plan* plan);
+
+/* ---- serving loop: continuous batching of single-sequence requests ----
+ * No reference counterpart (the reference folds caller-made batches only).
+ * A server owns n_workers engines (each with its own stream and arena) and as
+ * many worker threads.  Requests queue by (op, gamma / n_samples, length
+ * bucket); a free worker takes the queue with the oldest request, folds up to
+ * max_batch requests / max_batch_nt nucleotides of it as one batch and
+ * publishes the results.  A request's result equals the same request folded
+ * alone: logZ (cf_logz), MEA (cf_mea) and samples (cf_sample_seeded with the
+ * request's seed). */
+#define CF_ECANCELLED 6   /* serving: the request was cancelled or the server stopped */
+#define CF_OP_LOGZ   0
+#define CF_OP_MEA    1
+#define CF_OP_SAMPLE 2
+typedef struct cf_request {
+    int32_t op;          /* CF_OP_* */
+    int32_t n_samples;   /* CF_OP_SAMPLE: samples to draw */
+    float gamma;         /* CF_OP_MEA: gamma > 0 */
+    int32_t reserved;
+    uint64_t seed;       /* CF_OP_SAMPLE: Philox key of this request */
+} cf_request;
+typedef struct cf_server cf_server;
+int cf_server_create(const float* params32, const double* params64, int device,
+                     int32_t n_workers, cf_server** out);
+/* Joins the workers (running batches finish) and frees everything; no call on
+ * the server may be in progress or follow. */
+int cf_server_destroy(cf_server* server);
+/* Batch limits and length-bucket upper edges (nt, increasing).  Buckets whose
+ * upper edge is above long_len are long: only workers [0, long_workers) take
+ * them (and take short batches when no long request waits), so the other
+ * workers always serve short requests.  Only while no request is queued. */
+int cf_server_configure(cf_server* server, int32_t max_batch, int64_t max_batch_nt,
+                        int32_t long_len, int32_t long_workers, const int32_t* edges,
+                        int32_t n_edges);
+/* While paused, workers start no new batch (requests keep queueing). */
+int cf_server_pause(cf_server* server, int32_t on);
+/* Copies the sequence (and mask: NULL or len bytes, != 0 forces unpaired). */
+int cf_server_submit(cf_server* server, const cf_request* req, const uint8_t* seq,
+                     int32_t len, const uint8_t* mask, int64_t* ticket);
+/* Blocks until the request is done (timeout_ms < 0: no limit; on expiry
+ * CF_ETIMEOUT and the request stays), then returns its status and outputs and
+ * forgets the ticket: logZ in *logz_out, or the dot-bracket (L bytes) or the
+ * samples (n_samples * L bytes, sample-major) in out[0 .. out_cap). */
+int cf_server_wait(cf_server* server, int64_t ticket, int32_t timeout_ms,
+                   float* logz_out, char* out, int64_t out_cap);
+/* A request still queued is dropped; its wait returns CF_ECANCELLED. */
+int cf_server_cancel(cf_server* server, int64_t ticket);
+/* Open-loop replay: request k is submitted t_arrive[k] seconds after the call
+ * starts (non-decreasing), whatever the server's progress; the call returns
+ * when all are done.  Sequences and masks are laid out as in cf_logz; outputs
+ * go to logz_out[k] (logZ) or out[out_offsets[k] ..] (MEA: L bytes, samples:
+ * n_samples * L bytes); latency_ms[k] = completion - scheduled arrival;
+ * status_out[k] = the request's status. */
+int cf_server_replay(cf_server* server, int32_t n, const double* t_arrive,
+                     const cf_request* reqs, const uint8_t* seqs, const int64_t* offsets,
+                     const uint8_t* mask, const int64_t* out_offsets, float* logz_out,
+                     char* out, double* latency_ms, int32_t* status_out);
+/* stats[0..5] = batches, requests done, nucleotides done, cancelled,
+ * summed batch seconds over workers, requests queued now. */
+int cf_server_stats(cf_server* server, double* stats, int32_t n_stats);
 
 /* ---- MEA without device allocation ----
  * No reference counterpart: the reference allocates its device buffers with
