@@ -452,6 +452,145 @@ def serving_arm(args):
     return 0
 
 
+def side_arm(args):
+    """The other measured workloads, one JSON line each:
+      logz     : 1,000 x 128 nt (default_rng(0) bases, no mask), logZ folds/s through a
+                 device-resident plan (CUDA events, L2 flushed) and through logZ_batch;
+                 max |logZ - FP64 logZ|; the FP64 CPU engine (oracle) on all cores.
+      sampling : 4,096 sequences, lengths U{40..400} (default_rng(2)), 100 samples each,
+                 samples/s with the fold included, through sample_batch (host buffers)
+                 for the automatic, warp and grouped schedules.
+      grad     : 512 x 300 nt, soft unpaired bonuses N(0, 0.5) (default_rng(3)),
+                 gradients/s of logZ w.r.t. the 708 features and the bonuses (cf_grad +
+                 the host-side tying Jacobian)."""
+    import torch
+    import contrafold_gpu_gb300 as cg
+    from contrafold_gpu_gb300 import build as cbuild
+    from contrafold_gpu_gb300.engine import CF_JOB_LOGZ, CF_JOB_LOGZ64, Batch, Engine, Plan
+    cbuild.build()
+    P = cg.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    alpha = np.frombuffer(b"ACGU", np.uint8)
+    line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "impl": "ours"}
+    if args.workload == "logz":
+        n, L = 1000, 128
+        codes = np.random.default_rng(0).integers(0, 4, (n, L))
+        sb = alpha[codes].astype(np.uint8)
+        seqs = [bytes(r).decode() for r in sb]
+        offsets = np.arange(n + 1, dtype=np.int64) * L
+        d_seqs = torch.from_numpy(sb.reshape(-1).copy()).to(dev)
+        eng = Engine(P)
+        plan = Plan(eng, CF_JOB_LOGZ, offsets)
+        d_out = torch.empty(n, dtype=torch.float32, device=dev)
+        for _ in range(args.warmup):
+            plan.run(d_seqs.data_ptr(), 0, d_out.data_ptr(), 6.0, stream.cuda_stream)
+        plan.status()
+        ms = []
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1)
+                torch.cuda.synchronize(dev)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                plan.run(d_seqs.data_ptr(), 0, d_out.data_ptr(), 6.0, stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                ms.append(e0.elapsed_time(e1))
+        plan.status()
+        z32 = d_out.cpu().numpy().astype(np.float64)
+        p64 = Plan(eng, CF_JOB_LOGZ64, offsets)
+        d64 = torch.empty(n, dtype=torch.float64, device=dev)
+        p64.run(d_seqs.data_ptr(), 0, d64.data_ptr(), 6.0, stream.cuda_stream)
+        p64.status()
+        torch.cuda.synchronize(dev)
+        err = float(np.max(np.abs(z32 - d64.cpu().numpy())))
+        cg.logZ_batch(seqs[:64], P)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            cg.logZ_batch(seqs, P)
+        e2e = n * args.steps / (time.perf_counter() - t0)
+        from oracle import oracle as O
+        O.build()
+        cores = os.cpu_count() or 1
+        done, tt = 0, 0.0
+        while done < n and tt < 10.0:
+            sl = slice(done, min(n, done + 8 * cores))
+            t0 = time.perf_counter()
+            O.batch(O.JOB_LOGZ64, seqs[sl], P, None, 0.0, threads=cores)
+            tt += time.perf_counter() - t0
+            done = sl.stop
+        line.update({"metric": "logZ folds/s (1000 x 128 nt)", "value": n * len(ms) / (sum(ms) / 1e3),
+                     "unit": "folds/s", "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+                     "dtype": "f32", "config": {"workload": "logZ, 1000 x 128 nt i.i.d. ACGU (default_rng(0)), no mask",
+                                                "l2": "flushed between steps"},
+                     "logz_max_abs_err_vs_fp64": err,
+                     "e2e": {"value": e2e, "unit": "folds/s", "api": "contrafold_gpu_gb300.logZ_batch",
+                             "h2d_bytes_per_step": n * L + 8 * (n + 1), "d2h_bytes_per_step": 4 * n},
+                     "cpu_baseline": {"value": done / tt, "unit": "folds/s", "cores": cores, "kind": "port",
+                                      "sample": f"first {done} sequences, FP64 inside (cpu.py:165-275 restated), "
+                                                f"{cores} threads, {tt:.1f} s"},
+                     "clocks": clk.summary()})
+        plan.close(); p64.close(); eng.close()
+    elif args.workload == "sampling":
+        n, S = 4096, 100
+        rng = np.random.default_rng(2)
+        lens = rng.integers(40, 401, n)
+        seqs = [alpha[rng.integers(0, 4, int(L))].tobytes().decode() for L in lens]
+        B = Batch(seqs)
+        res = {}
+        with ClockSampler(0) as clk:
+            for sched in ("auto", "warp", "group"):
+                eng = Engine(P)
+                eng.set_schedule(sched)
+                for w in range(args.warmup):
+                    eng.sample(B, S, seed=w)
+                ts = []
+                for k in range(args.steps):
+                    t0 = time.perf_counter()
+                    eng.sample(B, S, seed=1000 + k)
+                    ts.append(time.perf_counter() - t0)
+                res[sched] = n * S / statistics.mean(ts)
+                eng.close()
+        line.update({"metric": "Boltzmann samples/s (fold included), 4096 seqs x U{40..400} nt x 100 samples",
+                     "value": res["auto"], "unit": "samples/s", "higher_is_better": True, "dtype": "f32",
+                     "schedules": res, "config": {"workload": "sampling, 4096 x U{40..400} nt (default_rng(2)), "
+                                                              "100 samples each, Philox (seed, seq, sample)",
+                                                  "api": "Engine.sample (host buffers, copies timed)"},
+                     "e2e": {"value": res["auto"], "unit": "samples/s", "h2d_bytes_per_step": int(B.total + 8 * (n + 1)),
+                             "d2h_bytes_per_step": int(B.total * S)},
+                     "clocks": clk.summary()})
+    else:
+        from contrafold_gpu_gb300 import grad
+        n, L = 512, 300
+        rng = np.random.default_rng(3)
+        codes = np.random.default_rng(0).integers(0, 4, (n, L))
+        seqs = [bytes(r).decode() for r in alpha[codes].astype(np.uint8)]
+        bonus = rng.normal(0, 0.5, (n, L)).astype(np.float32)
+        eng = Engine(P)
+        for _ in range(args.warmup):
+            grad.logz_grad(seqs, None, list(bonus), engine=eng)
+        ts = []
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                res = grad.logz_grad(seqs, None, list(bonus), engine=eng)
+                ts.append(time.perf_counter() - t0)
+        # sum_k P(k unpaired) + 2 E[#pairs] = L; its float32 residual, relative to L
+        ident = float(np.max([abs(res.d_bonus[b].sum() - (L - 2 * res.d_blob[b, 0:25].sum())) for b in range(n)])) / L
+        line.update({"metric": "logZ gradients/s (708 features + per-position bonus), 512 x 300 nt",
+                     "value": n / statistics.mean(ts), "unit": "gradients/s", "higher_is_better": True,
+                     "dtype": "f32 tables, f64 counts", "ms_per_step": 1e3 * statistics.mean(ts),
+                     "config": {"workload": "gradient, 512 x 300 nt i.i.d. ACGU, bonuses N(0,0.5) (default_rng(3))",
+                                "api": "grad.logz_grad (host buffers; tying Jacobian on the host)"},
+                     "identity_max_rel_err": ident, "clocks": clk.summary()})
+        eng.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -460,8 +599,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10000)
     ap.add_argument("--L", type=int, default=200)
-    ap.add_argument("--workload", choices=["mea", "serving"], default="mea",
-                    help="mea: the headline 200-nt MEA batch; serving: the open-loop request-stream sweep")
+    ap.add_argument("--workload", choices=["mea", "serving", "logz", "sampling", "grad"], default="mea",
+                    help="mea: the headline 200-nt MEA batch; serving: the open-loop request-stream sweep; "
+                         "logz / sampling / grad: the other measured workloads")
     ap.add_argument("--workers", type=int, default=6, help="serving: engines / worker threads")
     ap.add_argument("--long-workers", type=int, default=2, help="serving: workers that take long requests")
     ap.add_argument("--serve-n", type=int, default=20000, help="serving: requests of the saturation run")
@@ -470,6 +610,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "serving":
         return serving_arm(args)
+    if args.workload in ("logz", "sampling", "grad"):
+        return side_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return our_arm(args)

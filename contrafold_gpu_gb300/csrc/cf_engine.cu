@@ -890,6 +890,9 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
 int cf_plan_status(cf_plan* p) {
     if (!p) return fail(CF_EINVAL, "plan is NULL");
     int h = 0;
+    CF_CUDA(cudaSetDevice(p->eng->device));
+    // the runs may be on any stream, non-blocking ones included: wait for the device
+    CF_CUDA(cudaDeviceSynchronize());
     CF_CUDA(cudaMemcpy(&h, p->status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (h != CF_OK) return fail(h, "a kernel reported an internal limit (traceback stack/queue)");
     return CF_OK;
