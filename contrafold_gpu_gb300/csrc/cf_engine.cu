@@ -272,8 +272,10 @@ int check_batch(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets, int
 }
 
 int ensure_smem(cf_engine* eng, size_t bytes) {
-    if (bytes <= 48 * 1024) return CF_OK;
-    if (bytes <= eng->smem_optin) return CF_OK;
+    // set even below 48 KB: static shared memory (the cp.async chain ring)
+    // counts against the same 48 KB default limit
+    if (eng->smem_optin != 0 && bytes <= eng->smem_optin) return CF_OK;
+    bytes = std::max<size_t>(bytes, 48 * 1024);
     int dev_max = 0;
     CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device));
     if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");

@@ -161,6 +161,9 @@ __device__ __forceinline__ void step_items(SmemFold<R>* sm, int dB, int dA, GetP
     const int NB32 = (NB + 31) & ~31;
     for (int c = threadIdx.x; c < NB32 + NA; c += blockDim.x) {
         if (c < NB32) {
+            // B items fill whole warps (NB32 is a multiple of 32): the lanes
+            // holding a cell walk it together (see inside_B)
+            const unsigned lanes = __ballot_sync(0xffffffffu, c < NB);
             if (c >= NB) continue;
             int r = c, g = 0;
             for (;; ++g) {
@@ -168,7 +171,7 @@ __device__ __forceinline__ void step_items(SmemFold<R>* sm, int dB, int dA, GetP
                 if (dB <= L - 2) {
                     const PairList PLs = getpl(g);
                     const int o = PLs.poff[dB], cnt = PLs.poff[dB + 1] - o;
-                    if (r < cnt) { fB(g, (int)PLs.pl[o + r]); break; }
+                    if (r < cnt) { fB(g, (int)PLs.pl[o + r], lanes); break; }
                     r -= cnt;
                 }
             }
@@ -207,11 +210,11 @@ __device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, con
     for (int t = 0; t <= sm->Lmax + 1; ++t) {
         step_items(
             sm, t - 1, t <= sm->Lmax ? t : -1, getpl,
-            [&](int g, int i) {   // phase B(t-1): FC of a pairable cell
+            [&](int g, int i, unsigned lanes) {   // phase B(t-1): FC of a pairable cell
                 const SeqV Q = seq_v(sm, g);
                 const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
                 const R fm2 = V.FB[((t - 1) & 1) * V.fbs + i];
-                inside_B<S>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2);
+                inside_B<S>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2, lanes);
             },
             [&](int g, int i) {   // phase A(t): FM2, FM1, FM
                 const SeqV Q = seq_v(sm, g);
@@ -269,9 +272,9 @@ __device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArg
     for (int t = sm->Lmax; t >= 0; --t) {
         step_items(
             sm, t - 1, t, getpl,
-            [&](int g, int a) {   // phase B(t-1): FCo of a pairable cell
+            [&](int g, int a, unsigned lanes) {   // phase B(t-1): FCo of a pairable cell
                 const SeqV Q = seq_v(sm, g);
-                outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1);
+                outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
             },
             [&](int g, int a) {   // phase A(t): FMo, FM1o, FM2o
                 const SeqV Q = seq_v(sm, g);
@@ -302,18 +305,19 @@ __device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldA
         const float Z = T.F5[L];
         float* POST = T.FMo;
         float* dense = A.post_out ? A.post_out + A.post_offs[sm->idx[g]] : nullptr;
-        // pairable FC cells (i, i+d) <-> pairs (a, b) = (i, i+d+1), walked in
-        // list order (thread k takes entries k, k + blockDim, ...)
-        int c = threadIdx.x;
-        for (int d = 0; d <= L - 2; ++d) {
-            const int o = PLs.poff[d], cnt = PLs.poff[d + 1] - o;
-            for (; c < cnt; c += blockDim.x) {
-                const int a = PLs.pl[o + c], b = a + d + 1;
-                const float v = posterior_pair(&sm->tabs, &sm->poly, Q, T, Z, a, b);
-                POST[tri_off(d + 1, m) + a] = v;
-                if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
-            }
-            c -= cnt;
+        // pairable FC cells (i, i+d) <-> pairs (a, b) = (i, i+d+1), in list
+        // order, whole warps at a time (thread k takes entries k, k + blockDim, ...)
+        const int total = PLs.poff[L + 1];
+        const int lane = threadIdx.x & 31;
+        for (int c0 = threadIdx.x - lane; c0 < total; c0 += blockDim.x) {
+            const int c = c0 + lane;
+            const unsigned lanes = __ballot_sync(0xffffffffu, c < total);
+            if (c >= total) continue;
+            const int d = plist_diag(PLs, L, c);
+            const int a = PLs.pl[c], b = a + d + 1;
+            const float v = posterior_pair(&sm->tabs, &sm->poly, Q, T, Z, a, b, lanes);
+            POST[tri_off(d + 1, m) + a] = v;
+            if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
         }
     }
     __syncthreads();

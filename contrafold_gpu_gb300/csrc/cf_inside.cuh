@@ -112,41 +112,98 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 // ---------------------------------------------------------------------------
 // Prefetched sequential chains.  A bifurcation chain folds n terms x_k * y_k
 // (k ascending) into an accumulator; each step depends on the previous one,
-// but the operand loads do not.  The loop below keeps a rolling register
-// pipeline of 2*PF terms: the loads of block b+1 are issued before block b is
-// folded, so global-memory latency overlaps the dependent log-sum-exp chain
-// instead of stalling every step.  `ld(x, y)` loads the next term in k order
-// (it carries its own incremental addressing); `step(k, x, y)` folds term k.
+// but the operand loads do not.  `ld(px, py)` yields the addresses of the next
+// term's two operands in k order (it carries its own incremental addressing);
+// `step(k, x, y)` folds term k.  Three ways to run a chain, chosen per
+// translation unit (each .cu file is its own device module, compiled without
+// relocatable device code):
+//   CF_CHAIN_ASYNC = D > 0: a D-deep asynchronous-copy pipeline.  Each thread
+//     copies the operands of term k + D (cp.async, global -> shared) into its
+//     own slots of a ring of D + 1 shared-memory slots while it folds term k,
+//     so global-memory latency overlaps D dependent log-sum-exp steps without
+//     holding the prefetched values in registers.  The copy for term k + D
+//     goes to the slot read at term k - 1, whose value the fold of term k - 1
+//     has already consumed.  The module defines CF_CHAIN_THREADS (its block
+//     size); float chains only.
+//   CF_CHAIN_PF = PF > 0: a rolling register pipeline of 2*PF terms.
+//   both 0: load, then fold.
 // ---------------------------------------------------------------------------
-// Prefetch depths are per translation unit (each .cu file is its own device
-// module, compiled without relocatable device code): CF_CHAIN_PF terms per
-// pipeline block (0 = plain load-then-fold loop) and CF_WINDOW_LOOKAHEAD
-// window candidates in flight (0 or 2).
 #ifndef CF_CHAIN_PF
 #define CF_CHAIN_PF 4
 #endif
-#ifndef CF_WINDOW_LOOKAHEAD
-#define CF_WINDOW_LOOKAHEAD 2
+#ifndef CF_CHAIN_ASYNC
+#define CF_CHAIN_ASYNC 0
 #endif
 constexpr int kChainPF = CF_CHAIN_PF;
+constexpr int kChainAsync = CF_CHAIN_ASYNC;
+
+__device__ __forceinline__ void cp_async_f32(float* smem, const float* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+#if CF_CHAIN_ASYNC > 0
+// ring[slot][operand][thread]: consecutive threads use consecutive words
+__shared__ float cf_chain_ring[CF_CHAIN_ASYNC + 1][2][CF_CHAIN_THREADS];
+#endif
 
 template <typename R, class Ld, class Step>
 __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
+#if CF_CHAIN_ASYNC > 0
+    if constexpr (sizeof(R) == 4) {
+        constexpr int D = kChainAsync, NS = kChainAsync + 1;
+        const int tid = threadIdx.x;
+        auto issue = [&](int slot) {
+            const R *px, *py;
+            ld(px, py);
+            cp_async_f32(&cf_chain_ring[slot][0][tid], px);
+            cp_async_f32(&cf_chain_ring[slot][1][tid], py);
+        };
+#pragma unroll
+        for (int u = 0; u < D; ++u) {
+            if (u < n) issue(u);
+            cp_async_commit();
+        }
+        int rd = 0, wr = D;   // slots of term k and of term k + D
+        for (int k = 0; k < n; ++k) {
+            cp_async_wait<D - 1>();   // term k has landed
+            const R x = cf_chain_ring[rd][0][tid], y = cf_chain_ring[rd][1][tid];
+            if (k + D < n) issue(wr);
+            cp_async_commit();
+            step(k, x, y);
+            rd = rd + 1 == NS ? 0 : rd + 1;
+            wr = wr + 1 == NS ? 0 : wr + 1;
+        }
+        cp_async_wait<0>();
+        return;
+    }
+#endif
     if constexpr (kChainPF == 0) {
         for (int k = 0; k < n; ++k) {
-            R x, y;
-            ld(x, y);
-            step(k, x, y);
+            const R *px, *py;
+            ld(px, py);
+            step(k, *px, *py);
         }
     } else {
         R xa[kChainPF], ya[kChainPF], xb[kChainPF], yb[kChainPF];
+        auto load = [&](R& x, R& y) {
+            const R *px, *py;
+            ld(px, py);
+            x = *px;
+            y = *py;
+        };
 #pragma unroll
         for (int u = 0; u < kChainPF; ++u)
-            if (u < n) ld(xa[u], ya[u]);
+            if (u < n) load(xa[u], ya[u]);
         for (int k0 = 0; k0 < n; k0 += kChainPF) {
 #pragma unroll
             for (int u = 0; u < kChainPF; ++u)
-                if (k0 + kChainPF + u < n) ld(xb[u], yb[u]);
+                if (k0 + kChainPF + u < n) load(xb[u], yb[u]);
 #pragma unroll
             for (int u = 0; u < kChainPF; ++u)
                 if (k0 + u < n) step(k0 + u, xa[u], ya[u]);
@@ -155,29 +212,6 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
                 xa[u] = xb[u];
                 ya[u] = yb[u];
             }
-        }
-    }
-}
-
-// Drive a candidate generator `gen(c) -> bool`, loading each candidate with
-// `ld(c)` CF_WINDOW_LOOKAHEAD candidates ahead of `use(c, value)`.
-template <typename R, class C, class Gen, class Ld, class Use>
-__device__ __forceinline__ void lookahead_walk(Gen gen, Ld ld, Use use) {
-    if constexpr (CF_WINDOW_LOOKAHEAD == 0) {
-        C c;
-        while (gen(c)) use(c, ld(c));
-    } else {
-        C c0, c1, c2;
-        bool h0 = gen(c0);
-        R v0 = h0 ? ld(c0) : R(0);
-        bool h1 = h0 && gen(c1);
-        R v1 = h1 ? ld(c1) : R(0);
-        while (h0) {
-            const bool h2 = h1 && gen(c2);
-            const R v2 = h2 ? ld(c2) : R(0);
-            use(c0, v0);
-            c0 = c1; v0 = v1; h0 = h1;
-            c1 = c2; v1 = v2; h1 = h2;
         }
     }
 }
@@ -220,9 +254,9 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
         int s1 = 1, s2 = d - 1;
         prefetched_chain<R>(
             d - 1,
-            [&](R& x, R& y) {
-                x = T.FM1[o1];
-                y = T.FM[o2];
+            [&](const R*& x, const R*& y) {
+                x = T.FM1 + o1;
+                y = T.FM + o2;
                 o1 += m - s1;
                 o2 += s2 - m;           // FM[k+1][j]: span s2-1, one position right
                 ++s1;
@@ -270,10 +304,18 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
 // inner pairs (p+1, q) of the window, walked p ascending and, within a row,
 // q descending (highest set bit of the partner mask first) -- the reference's
 // order -- so only valid candidates cost work.
+//
+// `lanes` names the lanes of the warp that evaluate cells together (all of
+// them call inside_B with the same mask).  They walk the window in lockstep:
+// row by row (the rows and each row's q range depend only on d = j - i), and
+// within a row for as many slots as the lane with the most candidates has.  A
+// lane with fewer candidates idles in the remaining slots, so the warp never
+// splits into per-lane paths; each lane still folds exactly its own
+// candidates in the reference's order.
 template <class S, class QV>
 __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
                                          const QV& Q, const InTabs<typename S::Real>& T, int i, int j,
-                                         typename S::Real fm2) {
+                                         typename S::Real fm2, unsigned lanes) {
     using R = typename S::Real;
     const ParamView<R> P{tb->blob};
     const int L = Q.L, m = T.m, d = j - i;
@@ -281,40 +323,29 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
     const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
     const R jB = tb->jB[idx4(si, sj1, si1, sj)];
     R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
-    const int pmax = (i + CMAX < j) ? i + CMAX : j;
-    // Candidate generator: row p = i + l1 (ascending), q in [qlo, j] with
-    // qlo = max(p + 2, l1 + j - 30), pairable inner pairs (p+1, q) from the
-    // partner mask, highest q first.  Two candidates are kept in flight so the
-    // inner-value loads overlap the log-sum-exp of the current candidate.
-    int gp = i;
-    int gqlo = (gp + 2 > j - CMAX) ? gp + 2 : j - CMAX;
-    uint32_t gmsk = Q.window(gp + 1, gqlo, j - gqlo + 1);
-    auto gen = [&](int& pp, int& qq) -> bool {
-        while (gmsk == 0u) {
-            if (++gp > pmax) return false;
-            const int l1 = gp - i;
-            gqlo = (gp + 2 > l1 + j - CMAX) ? gp + 2 : l1 + j - CMAX;
-            gmsk = Q.window(gp + 1, gqlo, j - gqlo + 1);
-        }
-        const int bit = 31 - __clz(gmsk);
-        gmsk ^= 1u << bit;
-        pp = gp;
-        qq = gqlo + bit;
-        return true;
-    };
-    struct Cand { int p, q; };
-    lookahead_walk<R, Cand>(
-        [&](Cand& c) { return gen(c.p, c.q); },
-        [&](const Cand& c) -> R { return T.FC[tri_off(c.q - 2 - c.p, m) + c.p + 1]; },
-        [&](const Cand& c, R v) {
-            if (!(v > HALF)) return;
-            const int l1 = c.p - i, l2 = j - c.q, a = c.p + 1;
+    // rows p = i + l1, l1 = 0 .. min(30, d); row q range [qlo, j],
+    // qlo = max(p + 2, l1 + j - 30)
+    const int nrows = (d < CMAX ? d : CMAX) + 1;
+    const int nr = __reduce_max_sync(lanes, nrows);
+    for (int l1 = 0; l1 < nr; ++l1) {
+        const int p = i + l1;
+        const int qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
+        uint32_t msk = l1 < nrows ? Q.window(p + 1, qlo, j - qlo + 1) : 0u;
+        const int slots = __reduce_max_sync(lanes, __popc(msk));
+        for (int k = 0; k < slots; ++k) {
+            if (msk == 0u) continue;
+            const int bit = 31 - __clz(msk);
+            msk ^= 1u << bit;
+            const int q = qlo + bit;
+            const R v = T.FC[tri_off(q - 2 - p, m) + p + 1];
+            if (!(v > HALF)) continue;
+            const int l2 = j - q, a = p + 1;
             R e;
             if (l1 == 0 && l2 == 0) {
                 e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
             } else {
-                const int sq = Q.s[c.q], sa = Q.s[a];
-                const R jB2 = tb->jB[idx4(sq, sa, Q.s[c.q + 1], Q.s[c.p])];
+                const int sq = Q.s[q], sa = Q.s[a];
+                const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
                 R snuc = R(0);
                 if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
                 else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
@@ -322,7 +353,8 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
                 e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
             }
             acc = sr.plus(acc, S::add(e, v));
-        });
+        }
+    }
     if (fm2 > HALF) {
         const R jA = junctionA<S>(P, L, Q, i, j);
         acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));

@@ -50,9 +50,9 @@ __device__ __forceinline__ void mea_cell(const QV& Q, const float* __restrict__ 
         int s1 = 1, s2 = j - i - 1;
         prefetched_chain<float>(
             j - i - 1,
-            [&](float& x, float& y) {
-                x = score[o1];
-                y = score[o2];
+            [&](const float*& x, const float*& y) {
+                x = score + o1;
+                y = score + o2;
                 o1 += m - s1;
                 o2 += s2 - m;
                 ++s1;

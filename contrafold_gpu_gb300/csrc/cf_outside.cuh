@@ -156,7 +156,7 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
         int first = 1;
         prefetched_chain<float>(
             K,
-            [&](float& x, float& y) {
+            [&](const float*& x, const float*& y) {
                 if (kl == n1) {
                     w = n2;
                     addr1 = tri_off(t + n2, m) + a;
@@ -164,8 +164,8 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
                     tab2 = T.FM;
                     first = 0;
                 }
-                x = T.FM2o[addr1];
-                y = tab2[addr2];
+                x = T.FM2o + addr1;
+                y = tab2 + addr2;
                 addr1 -= (m - t - w + 1) - first;
                 addr2 -= (m - w + 1) - first;
                 --w;
@@ -202,8 +202,11 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
 //     each row walks the partner mask of position i over j+1 = b+2 ..
 //     b+2+(30-l1), highest bit first.  Source (a-1, b+1) first contributes
 //     through FM1o (block 2, cpu.py:708-714), then through block 3.
+// `lanes`: the lanes evaluating cells together, walked in lockstep as in
+// inside_B (rows from the largest l1max among them, per row as many slots as
+// the lane with the most candidates).
 __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>* __restrict__ tb,
-                                          const SeqV& Q, const OutTabs& T, int a, int b) {
+                                          const SeqV& Q, const OutTabs& T, int a, int b, unsigned lanes) {
     const ParamView<float> P{tb->blob};
     const int L = Q.L, m = T.m, t = b - a;
     const int sa = Q.s[a], sb1 = Q.s[b + 1];
@@ -220,76 +223,54 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
     // jB of the inner pair (p+1, q) = (a, b+1): hc[s[q]][s[p+1]] + tm[s[q]][s[p+1]][s[q+1]][s[p]]
     const float jB2 = tb->jB[idx4(sb1, sa, Q.s[b + 2], Q.s[a - 1])];
     const int l1max = (a - 2 < CMAX) ? a - 2 : CMAX;   // i = a-1-l1 >= 1
-    // Generator over (kind, l1, j): rows l1 = l1max .. 0, j descending within a
-    // row (highest mask bit first); in row 0 the FM1o term of source
-    // (a-1, b+1) (kind 1) comes after the l2 >= 1 candidates and before l2 = 0.
-    int gl1 = l1max;
-    uint32_t gmsk = 0u;
-    bool ev_pending = false, bit0_pending = false;
     auto rowmask = [&](int l1) -> uint32_t {
         const int jmax = (b + 1 + CMAX - l1 < L - 1) ? b + 1 + CMAX - l1 : L - 1;
         return Q.window(a - 1 - l1, b + 2, jmax - b);
     };
-    auto enter_row = [&]() {
-        const uint32_t m0 = rowmask(gl1);
-        if (gl1 == 0) {
-            gmsk = m0 & ~1u;
-            ev_pending = b + 1 < L;
-            bit0_pending = (m0 & 1u) != 0u;
+    // single-branch source (i, j) = (a-1-l1, j) with l2 = j - (b+1)
+    auto source = [&](int l1, int j) {
+        const int i = a - 1 - l1;
+        const float v = T.FCo[tri_off(j - i, m) + i];
+        if (!(v > CF_HALF32)) return;
+        const int l2 = j - (b + 1);
+        const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j];
+        float e;
+        if (l1 == 0 && l2 == 0) {
+            e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[j + 1], si1, sj));
         } else {
-            gmsk = m0;
+            const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
+            float snuc = 0.0f;
+            if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+            else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+            else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+            e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), bp_ab), jBij), jB2), snuc);
         }
+        acc = sr.plus(acc, __fadd_rn(v, e));
     };
-    if (gl1 >= 0) enter_row();
-    auto gen = [&](int& kind, int& l1, int& j) -> bool {
-        if (gl1 < 0) return false;
-        while (true) {
-            if (gmsk) {
-                const int bit = 31 - __clz(gmsk);
-                gmsk ^= 1u << bit;
-                kind = 0; l1 = gl1; j = b + 1 + bit;
-                return true;
-            }
-            if (gl1 == 0) {
-                if (ev_pending) { ev_pending = false; kind = 1; l1 = 0; j = b + 1; return true; }
-                if (bit0_pending) { bit0_pending = false; kind = 0; l1 = 0; j = b + 1; return true; }
-                gl1 = -1;
-                return false;
-            }
-            --gl1;
-            enter_row();
+    const int lm = __reduce_max_sync(lanes, l1max + 1) - 1;
+    uint32_t m0 = 0u;
+    for (int l1 = lm; l1 >= 0; --l1) {
+        uint32_t msk = l1 <= l1max ? rowmask(l1) : 0u;
+        if (l1 == 0) {
+            m0 = msk;
+            msk &= ~1u;   // the stacking source comes after the FM1o term
         }
-    };
-    struct Cand { int kind, l1, j; };
-    lookahead_walk<float, Cand>(
-        [&](Cand& c) { return gen(c.kind, c.l1, c.j); },
-        [&](const Cand& c) -> float {
-            if (c.kind == 1) return T.FM1o[tri_off(t + 2, m) + a - 1];
-            const int i = a - 1 - c.l1;
-            return T.FCo[tri_off(c.j - i, m) + i];
-        },
-        [&](const Cand& c, float v) {
-            if (c.kind == 1) {
-                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
-                acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v, jAji), P.mp()), bp_ab));
-                return;
-            }
-            if (!(v > CF_HALF32)) return;
-            const int i = a - 1 - c.l1, l2 = c.j - (b + 1);
-            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[c.j];
-            float e;
-            if (c.l1 == 0 && l2 == 0) {
-                e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[c.j + 1], si1, sj));
-            } else {
-                const float jBij = tb->jB[idx4(si, Q.s[c.j + 1], si1, sj)];
-                float snuc = 0.0f;
-                if (c.l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                else if (c.l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                else if (c.l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(c.l1, l2), bp_ab), jBij), jB2), snuc);
-            }
-            acc = sr.plus(acc, __fadd_rn(v, e));
-        });
+        const int slots = __reduce_max_sync(lanes, __popc(msk));
+        for (int k = 0; k < slots; ++k) {
+            if (msk == 0u) continue;
+            const int bit = 31 - __clz(msk);
+            msk ^= 1u << bit;
+            source(l1, b + 1 + bit);
+        }
+    }
+    if (l1max >= 0) {
+        if (b + 1 < L) {
+            const float v = T.FM1o[tri_off(t + 2, m) + a - 1];
+            const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
+            acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v, jAji), P.mp()), bp_ab));
+        }
+        if (m0 & 1u) source(0, b + 1);
+    }
     T.FCo[tri_off(t, m) + a] = acc;
 }
 
@@ -299,84 +280,72 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
 // each iff pairable(i, j+1) and its outside value is live; source (a-1, b)
 // adds its multiloop (FM1o) term right after its stacking term; the exterior
 // term comes last.  Returns the clipped value.
+// `lanes`: the lanes evaluating pairs together, walked in lockstep as in
+// inside_B.
 __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restrict__ tb, const PolyTables* pt,
-                                                const SeqV& Q, const OutTabs& T, float Z, int a, int b) {
+                                                const SeqV& Q, const OutTabs& T, float Z, int a, int b,
+                                                unsigned lanes) {
     const ParamView<float> P{tb->blob};
     const int L = Q.L, m = T.m;
     const float fcin = T.FC[tri_off(b - 1 - a, m) + a];
-    if (!(fcin > CF_HALF32)) return 0.0f;
+    const bool live = fcin > CF_HALF32;
     const int sa = Q.s[a], sb = Q.s[b];
     const float bp_ab = P.bp(sa, sb);
     // jB of the inner pair (p+1, q) = (a, b)
     const float jB2 = tb->jB[idx4(sb, sa, Q.s[b + 1], Q.s[a - 1])];
     float post = 0.0f;
-    const int l1max = (a - 2 < CMAX) ? a - 2 : CMAX;   // i = a-1-l1 >= 1
-    // Generator over (kind, l1, j): rows l1 = 0 .. l1max, j ascending within a
-    // row (lowest mask bit first); in row 0 the multiloop term of source
-    // (a-1, b) (kind 1) follows that source's stacking term (l2 = 0).
-    int gl1 = 0;
-    uint32_t gmsk = 0u;
-    bool ev_pending = false, bit0_pending = false;
+    const int l1max = live ? ((a - 2 < CMAX) ? a - 2 : CMAX) : -1;   // i = a-1-l1 >= 1
     auto rowmask = [&](int l1) -> uint32_t {
         const int jmax = (b + CMAX - l1 < L - 1) ? b + CMAX - l1 : L - 1;
         return Q.window(a - 1 - l1, b + 1, jmax - b + 1);
     };
-    if (l1max >= 0) {
-        const uint32_t m0 = rowmask(0);
-        bit0_pending = (m0 & 1u) != 0u;
-        ev_pending = b < L;
-        gmsk = m0 & ~1u;
-    } else {
-        gl1 = 1;   // no rows
-    }
-    auto gen = [&](int& kind, int& l1, int& j) -> bool {
-        while (true) {
-            if (gl1 == 0 && bit0_pending) { bit0_pending = false; kind = 0; l1 = 0; j = b; return true; }
-            if (gl1 == 0 && ev_pending) { ev_pending = false; kind = 1; l1 = 0; j = b; return true; }
-            if (gmsk) {
-                const int bit = __ffs(gmsk) - 1;
-                gmsk &= gmsk - 1u;
-                kind = 0; l1 = gl1; j = b + bit;
-                return true;
-            }
-            if (++gl1 > l1max) return false;
-            gmsk = rowmask(gl1);
+    // single-branch source (i, j) = (a-1-l1, j), l2 = j - b
+    auto source = [&](int l1, int j) {
+        const int i = a - 1 - l1;
+        const float outside = __fsub_rn(T.FCo[tri_off(j - i, m) + i], Z);
+        if (!(outside > CF_HALF32)) return;
+        const int l2 = j - b;
+        const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j];
+        float e;
+        if (l1 == 0 && l2 == 0) {
+            e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j + 1], si1, sj)), fcin);
+        } else {
+            const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
+            float snuc = 0.0f;
+            if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+            else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+            else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+            e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l1, l2)), fcin), bp_ab), jB2), snuc);
         }
+        post = __fadd_rn(post, fexp32(pt, e));
     };
-    struct Cand { int kind, l1, j; };
-    lookahead_walk<float, Cand>(
-        [&](Cand& c) { return gen(c.kind, c.l1, c.j); },
-        [&](const Cand& c) -> float {
-            if (c.kind == 1) return T.FM1o[tri_off(b - a + 1, m) + a - 1];
-            const int i = a - 1 - c.l1;
-            return T.FCo[tri_off(c.j - i, m) + i];
-        },
-        [&](const Cand& c, float v) {
-            if (c.kind == 1) {
-                if (v > CF_HALF32) {
-                    const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
-                    const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, fcin), jAji), P.mp()), bp_ab), Z);
-                    post = __fadd_rn(post, fexp32(pt, x));
-                }
-                return;
+    // row 0: the stacking source (a-1, b), its multiloop term, then j ascending
+    uint32_t m0 = 0u;
+    if (l1max >= 0) {
+        m0 = rowmask(0);
+        if (m0 & 1u) source(0, b);
+        if (b < L) {
+            const float v = T.FM1o[tri_off(b - a + 1, m) + a - 1];
+            if (v > CF_HALF32) {
+                const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b);
+                const float x = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, fcin), jAji), P.mp()), bp_ab), Z);
+                post = __fadd_rn(post, fexp32(pt, x));
             }
-            const float outside = __fsub_rn(v, Z);
-            if (!(outside > CF_HALF32)) return;
-            const int i = a - 1 - c.l1, l2 = c.j - b;
-            const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[c.j];
-            float e;
-            if (c.l1 == 0 && l2 == 0) {
-                e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[c.j + 1], si1, sj)), fcin);
-            } else {
-                const float jBij = tb->jB[idx4(si, Q.s[c.j + 1], si1, sj)];
-                float snuc = 0.0f;
-                if (c.l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                else if (c.l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                else if (c.l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(c.l1, l2)), fcin), bp_ab), jB2), snuc);
-            }
-            post = __fadd_rn(post, fexp32(pt, e));
-        });
+        }
+        m0 &= ~1u;
+    }
+    const int lm = __reduce_max_sync(lanes, l1max + 1) - 1;
+    for (int l1 = 0; l1 <= lm; ++l1) {
+        uint32_t msk = l1 == 0 ? m0 : (l1 <= l1max ? rowmask(l1) : 0u);
+        const int slots = __reduce_max_sync(lanes, __popc(msk));
+        for (int k = 0; k < slots; ++k) {
+            if (msk == 0u) continue;
+            const int bit = __ffs(msk) - 1;
+            msk &= msk - 1u;
+            source(l1, b + bit);
+        }
+    }
+    if (!live) return 0.0f;
     const float outside = __fsub_rn(T.F5o[b], Z);
     const float f5k = T.F5[a - 1];
     if (outside > CF_HALF32 && f5k > CF_HALF32) {

@@ -72,6 +72,17 @@ struct PairList {
     int16_t* pl;     // [tri_size(L)]
 };
 
+// Diagonal d of list entry c (poff[d] <= c < poff[d+1]), 0 <= c < poff[L+1].
+__device__ __forceinline__ int plist_diag(const PairList& P, int L, int c) {
+    int lo = 0, hi = L;   // the largest d with poff[d] <= c
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.poff[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ PairList plist_at(float* base, int L) {
     PairList P;
     P.poff = reinterpret_cast<int32_t*>(base);

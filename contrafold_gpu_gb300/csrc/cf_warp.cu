@@ -16,8 +16,18 @@
 // This module runs one sequence per warp: 32+ independent warps per SM hide
 // memory latency, so the chains use plain loops (no register pipelines) and a
 // small register budget keeps the SM full.
+#ifndef CF_CHAIN_PF
 #define CF_CHAIN_PF 0
-#define CF_WINDOW_LOOKAHEAD 0
+#endif
+// bifurcation-chain operands arrive through a CF_CHAIN_ASYNC-deep cp.async
+// ring in shared memory (hides DRAM latency without prefetch registers)
+#ifndef CF_CHAIN_ASYNC
+#define CF_CHAIN_ASYNC 8
+#endif
+#define CF_CHAIN_THREADS 256
+#ifndef CF_WARP_MIN_BLOCKS
+#define CF_WARP_MIN_BLOCKS 4
+#endif
 #include "cf_mea.cuh"
 #include "cf_outside.cuh"
 #include "cf_sample.cuh"
@@ -99,9 +109,12 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
             const int dB = t - 1;
             if (dB >= 0 && dB <= L - 2) {
                 const int o = PLs.poff[dB], cnt = PLs.poff[dB + 1] - o;
-                for (int k = lane; k < cnt; k += 32) {
+                for (int k0 = 0; k0 < cnt; k0 += 32) {
+                    const int k = k0 + lane;
+                    const unsigned lanes = __ballot_sync(0xffffffffu, k < cnt);
+                    if (k >= cnt) continue;
                     const int i = PLs.pl[o + k];
-                    inside_B<S>(sr, &sm->tabs, Q, T, i, i + dB, FB[(dB & 1) * fbs + i]);
+                    inside_B<S>(sr, &sm->tabs, Q, T, i, i + dB, FB[(dB & 1) * fbs + i], lanes);
                 }
             }
             if (t <= L)
@@ -147,9 +160,12 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
         const int dB = t - 1;
         if (dB >= 0 && dB <= L - 2) {
             const int o = PLs.poff[dB], cnt = PLs.poff[dB + 1] - o;
-            for (int k = lane; k < cnt; k += 32) {
+            for (int k0 = 0; k0 < cnt; k0 += 32) {
+                const int k = k0 + lane;
+                const unsigned lanes = __ballot_sync(0xffffffffu, k < cnt);
+                if (k >= cnt) continue;
                 const int a = PLs.pl[o + k];
-                outside_B(sr, &sm->tabs, Q, O, a, a + dB);
+                outside_B(sr, &sm->tabs, Q, O, a, a + dB, lanes);
             }
         }
         for (int a = lane; a <= L - t; a += 32) outside_A_merged(sr, &sm->tabs, Q, O, a, a + t);
@@ -165,14 +181,16 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
     if (dense != nullptr)
         for (int64_t c = lane; c < (int64_t)L * L; c += 32) dense[c] = 0.0f;
     __syncwarp();
-    for (int d = 0; d <= L - 2; ++d) {
-        const int o = PLs.poff[d], cnt = PLs.poff[d + 1] - o;
-        for (int k = lane; k < cnt; k += 32) {
-            const int a = PLs.pl[o + k], b = a + d + 1;
-            const float v = posterior_pair(&sm->tabs, &sm->poly, Q, O, Z, a, b);
-            POST[tri_off(d + 1, m) + a] = v;
-            if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
-        }
+    const int total = PLs.poff[L + 1];
+    for (int c0 = 0; c0 < total; c0 += 32) {
+        const int c = c0 + lane;
+        const unsigned lanes = __ballot_sync(0xffffffffu, c < total);
+        if (c >= total) continue;
+        const int d = plist_diag(PLs, L, c);
+        const int a = PLs.pl[c], b = a + d + 1;
+        const float v = posterior_pair(&sm->tabs, &sm->poly, Q, O, Z, a, b, lanes);
+        POST[tri_off(d + 1, m) + a] = v;
+        if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
     }
     __syncwarp();
     if constexpr (MODE == kWarpBpp) {
@@ -202,7 +220,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarpThreads, 4) k_fold_warp(WarpArgs A) {
+__global__ void __launch_bounds__(kWarpThreads, CF_WARP_MIN_BLOCKS) k_fold_warp(WarpArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<WarpSmemHead*>(smem_raw);
     load_tabs(&sm->tabs, A.blob32);
