@@ -216,6 +216,40 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
     }
 }
 
+// One row of a lockstep window walk (see inside_B): every lane of the group
+// runs `slots` iterations (the largest candidate count among them) and takes
+// the set bits of its own mask, highest first (HI) or lowest first; the
+// table value of the next candidate, `ld(bit)`, is loaded before the current
+// one is used, `use(bit, v)`.
+template <bool HI, typename R, class Ld, class Use>
+__device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use use) {
+    auto take = [&](int& bit) -> bool {
+        if (msk == 0u) return false;
+        if constexpr (HI) {
+            bit = 31 - __clz(msk);
+            msk ^= 1u << bit;
+        } else {
+            bit = __ffs(msk) - 1;
+            msk &= msk - 1u;
+        }
+        return true;
+    };
+    int bit = 0;
+    R v = R(0);
+    bool h = take(bit);
+    if (h) v = ld(bit);
+    for (int k = 0; k < slots; ++k) {
+        int bn = 0;
+        R vn = R(0);
+        const bool hn = take(bn);
+        if (hn) vn = ld(bn);
+        if (h) use(bit, v);
+        h = hn;
+        bit = bn;
+        v = vn;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Two-phase cell evaluation.  On diagonal t:
 //   phase A (every cell): FM2 (kept for phase B), FM1, FM -- they read FC only
@@ -332,28 +366,26 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         const int qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
         uint32_t msk = l1 < nrows ? Q.window(p + 1, qlo, j - qlo + 1) : 0u;
         const int slots = __reduce_max_sync(lanes, __popc(msk));
-        for (int k = 0; k < slots; ++k) {
-            if (msk == 0u) continue;
-            const int bit = 31 - __clz(msk);
-            msk ^= 1u << bit;
-            const int q = qlo + bit;
-            const R v = T.FC[tri_off(q - 2 - p, m) + p + 1];
-            if (!(v > HALF)) continue;
-            const int l2 = j - q, a = p + 1;
-            R e;
-            if (l1 == 0 && l2 == 0) {
-                e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
-            } else {
-                const int sq = Q.s[q], sa = Q.s[a];
-                const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
-                R snuc = R(0);
-                if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
-                e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
-            }
-            acc = sr.plus(acc, S::add(e, v));
-        }
+        lockstep_row<true, R>(
+            msk, slots, [&](int bit) -> R { return T.FC[tri_off(qlo + bit - 2 - p, m) + p + 1]; },
+            [&](int bit, R v) {
+                if (!(v > HALF)) return;
+                const int q = qlo + bit;
+                const int l2 = j - q, a = p + 1;
+                R e;
+                if (l1 == 0 && l2 == 0) {
+                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
+                } else {
+                    const int sq = Q.s[q], sa = Q.s[a];
+                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
+                    R snuc = R(0);
+                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
+                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
+                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
+                }
+                acc = sr.plus(acc, S::add(e, v));
+            });
     }
     if (fm2 > HALF) {
         const R jA = junctionA<S>(P, L, Q, i, j);

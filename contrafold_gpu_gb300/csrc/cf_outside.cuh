@@ -228,9 +228,12 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
         return Q.window(a - 1 - l1, b + 2, jmax - b);
     };
     // single-branch source (i, j) = (a-1-l1, j) with l2 = j - (b+1)
-    auto source = [&](int l1, int j) {
+    auto src_val = [&](int l1, int j) -> float {
         const int i = a - 1 - l1;
-        const float v = T.FCo[tri_off(j - i, m) + i];
+        return T.FCo[tri_off(j - i, m) + i];
+    };
+    auto source = [&](int l1, int j, float v) {
+        const int i = a - 1 - l1;
         if (!(v > CF_HALF32)) return;
         const int l2 = j - (b + 1);
         const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j];
@@ -256,12 +259,9 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             msk &= ~1u;   // the stacking source comes after the FM1o term
         }
         const int slots = __reduce_max_sync(lanes, __popc(msk));
-        for (int k = 0; k < slots; ++k) {
-            if (msk == 0u) continue;
-            const int bit = 31 - __clz(msk);
-            msk ^= 1u << bit;
-            source(l1, b + 1 + bit);
-        }
+        lockstep_row<true, float>(
+            msk, slots, [&](int bit) { return src_val(l1, b + 1 + bit); },
+            [&](int bit, float v) { source(l1, b + 1 + bit, v); });
     }
     if (l1max >= 0) {
         if (b + 1 < L) {
@@ -269,7 +269,7 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
             acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v, jAji), P.mp()), bp_ab));
         }
-        if (m0 & 1u) source(0, b + 1);
+        if (m0 & 1u) source(0, b + 1, src_val(0, b + 1));
     }
     T.FCo[tri_off(t, m) + a] = acc;
 }
@@ -300,9 +300,13 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
         return Q.window(a - 1 - l1, b + 1, jmax - b + 1);
     };
     // single-branch source (i, j) = (a-1-l1, j), l2 = j - b
-    auto source = [&](int l1, int j) {
+    auto src_val = [&](int l1, int j) -> float {
         const int i = a - 1 - l1;
-        const float outside = __fsub_rn(T.FCo[tri_off(j - i, m) + i], Z);
+        return T.FCo[tri_off(j - i, m) + i];
+    };
+    auto source = [&](int l1, int j, float fco) {
+        const int i = a - 1 - l1;
+        const float outside = __fsub_rn(fco, Z);
         if (!(outside > CF_HALF32)) return;
         const int l2 = j - b;
         const int si = Q.s[i], si1 = Q.s[i + 1], sj = Q.s[j];
@@ -323,7 +327,7 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
     uint32_t m0 = 0u;
     if (l1max >= 0) {
         m0 = rowmask(0);
-        if (m0 & 1u) source(0, b);
+        if (m0 & 1u) source(0, b, src_val(0, b));
         if (b < L) {
             const float v = T.FM1o[tri_off(b - a + 1, m) + a - 1];
             if (v > CF_HALF32) {
@@ -338,12 +342,9 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
     for (int l1 = 0; l1 <= lm; ++l1) {
         uint32_t msk = l1 == 0 ? m0 : (l1 <= l1max ? rowmask(l1) : 0u);
         const int slots = __reduce_max_sync(lanes, __popc(msk));
-        for (int k = 0; k < slots; ++k) {
-            if (msk == 0u) continue;
-            const int bit = __ffs(msk) - 1;
-            msk &= msk - 1u;
-            source(l1, b + bit);
-        }
+        lockstep_row<false, float>(
+            msk, slots, [&](int bit) { return src_val(l1, b + bit); },
+            [&](int bit, float v) { source(l1, b + bit, v); });
     }
     if (!live) return 0.0f;
     const float outside = __fsub_rn(T.F5o[b], Z);
