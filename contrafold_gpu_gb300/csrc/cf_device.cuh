@@ -99,6 +99,12 @@ __host__ __device__ __forceinline__ Arena64 arena64(int L) {
 // memory (one float4 per segment) because lanes of a warp fall into different
 // segments.  The evaluation order ((c0*d + c1)*d + c2)*d + c3 is the
 // reference's.
+//
+// Segment lookup: with u = 4d (exact), bin = floor(u) in 0..47 holds at most
+// one boundary (boundaries are >= 0.86 apart, bins 0.25 wide), so
+// seg = (boundaries below the bin) + (d >= the boundary inside the bin), read
+// from a 48-entry table -- the same count as comparing d with all seven.
+// Fast_Exp uses the same scheme on u = -4x over its five boundaries.
 // ---------------------------------------------------------------------------
 #define LSE_T0 ((float)0.6615367791)
 #define LSE_T1 ((float)1.6320158198)
@@ -116,34 +122,64 @@ __host__ __device__ __forceinline__ Arena64 arena64(int L) {
 #define FEXP_T4 ((float)-1.4805375919)
 #define FEXP_T5 ((float)-0.6725053211)
 
+constexpr int kLseBins = 48;    // 0.25-wide bins of d over [0, 12)
+constexpr int kFexpBins = 40;   // 0.25-wide bins of -x over [0, 10)
+
 struct PolyTables {
     float4 lse[8];
     float4 fexp[6];
+    float2 lse_bin[kLseBins];     // {boundary inside the bin or +FLT_MAX, int bits: boundaries below}
+    float2 fexp_bin[kFexpBins];   // {-boundary inside the bin or -FLT_MAX, int bits: boundaries above}
 };
 
 __device__ __forceinline__ void load_poly_tables(PolyTables* t) {
-    const int k = threadIdx.x;
-    if (k < 8) {
-        const float c[8][4] = {
-            {(float)-0.0065591595, (float)0.1276442762, (float)0.4996554598, (float)0.6931542306},
-            {(float)-0.0155157557, (float)0.1446775699, (float)0.4882939746, (float)0.6958092989},
-            {(float)-0.0128909247, (float)0.1301028251, (float)0.5150398748, (float)0.6795585882},
-            {(float)-0.0072142647, (float)0.0877540853, (float)0.6208708362, (float)0.5909675829},
-            {(float)-0.0031455354, (float)0.0467229449, (float)0.7592532310, (float)0.4348794399},
-            {(float)-0.0010110698, (float)0.0185943421, (float)0.8831730747, (float)0.2523695427},
-            {(float)-0.0001962780, (float)0.0046084408, (float)0.9634431978, (float)0.0983148903},
-            {(float)-0.0000113994, (float)0.0003734731, (float)0.9959107193, (float)0.0149855051}};
-        t->lse[k] = make_float4(c[k][0], c[k][1], c[k][2], c[k][3]);
-    } else if (k < 14) {
-        const float c[6][4] = {
-            {(float)0.0000803850, (float)0.0021627428, (float)0.0194708555, (float)0.0588080014},
-            {(float)0.0013889414, (float)0.0244676474, (float)0.1471290604, (float)0.3042757740},
-            {(float)0.0072335607, (float)0.0906002677, (float)0.3983111356, (float)0.6245959221},
-            {(float)0.0232410351, (float)0.2085645908, (float)0.6906367911, (float)0.8682322329},
-            {(float)0.0573782771, (float)0.3580258429, (float)0.9121133217, (float)0.9793091728},
-            {(float)0.1199175927, (float)0.4815668234, (float)0.9975991939, (float)0.9999505077}};
-        const int s = k - 8;
-        t->fexp[s] = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
+    for (int k = threadIdx.x; k < 16 + kLseBins + kFexpBins; k += blockDim.x) {
+        if (k < 8) {
+            const float c[8][4] = {
+                {(float)-0.0065591595, (float)0.1276442762, (float)0.4996554598, (float)0.6931542306},
+                {(float)-0.0155157557, (float)0.1446775699, (float)0.4882939746, (float)0.6958092989},
+                {(float)-0.0128909247, (float)0.1301028251, (float)0.5150398748, (float)0.6795585882},
+                {(float)-0.0072142647, (float)0.0877540853, (float)0.6208708362, (float)0.5909675829},
+                {(float)-0.0031455354, (float)0.0467229449, (float)0.7592532310, (float)0.4348794399},
+                {(float)-0.0010110698, (float)0.0185943421, (float)0.8831730747, (float)0.2523695427},
+                {(float)-0.0001962780, (float)0.0046084408, (float)0.9634431978, (float)0.0983148903},
+                {(float)-0.0000113994, (float)0.0003734731, (float)0.9959107193, (float)0.0149855051}};
+            t->lse[k] = make_float4(c[k][0], c[k][1], c[k][2], c[k][3]);
+        } else if (k < 14) {
+            const float c[6][4] = {
+                {(float)0.0000803850, (float)0.0021627428, (float)0.0194708555, (float)0.0588080014},
+                {(float)0.0013889414, (float)0.0244676474, (float)0.1471290604, (float)0.3042757740},
+                {(float)0.0072335607, (float)0.0906002677, (float)0.3983111356, (float)0.6245959221},
+                {(float)0.0232410351, (float)0.2085645908, (float)0.6906367911, (float)0.8682322329},
+                {(float)0.0573782771, (float)0.3580258429, (float)0.9121133217, (float)0.9793091728},
+                {(float)0.1199175927, (float)0.4815668234, (float)0.9975991939, (float)0.9999505077}};
+            const int s = k - 8;
+            t->fexp[s] = make_float4(c[s][0], c[s][1], c[s][2], c[s][3]);
+        } else if (k < 16 + kLseBins) {
+            if (k >= 16) {
+                const int b = k - 16;
+                const float lo = __fmul_rn((float)b, 0.25f), hi = __fmul_rn((float)(b + 1), 0.25f);
+                const float T[7] = {LSE_T0, LSE_T1, LSE_T2, LSE_T3, LSE_T4, LSE_T5, LSE_T6};
+                int base = 0;
+                float inner = 3.402823466e38f;
+                for (int i = 0; i < 7; ++i) {
+                    if (T[i] <= lo) ++base;
+                    else if (T[i] < hi) inner = T[i];
+                }
+                t->lse_bin[b] = make_float2(inner, __int_as_float(base));
+            }
+        } else if (k < 16 + kLseBins + kFexpBins) {
+            const int b = k - 16 - kLseBins;
+            const float lo = __fmul_rn((float)b, 0.25f), hi = __fmul_rn((float)(b + 1), 0.25f);
+            const float U[5] = {-FEXP_T1, -FEXP_T2, -FEXP_T3, -FEXP_T4, -FEXP_T5};
+            int base = 0;   // boundaries U_k >= hi: u <= U_k for every u of the bin
+            float inner = -3.402823466e38f;
+            for (int i = 0; i < 5; ++i) {
+                if (U[i] >= hi) ++base;
+                else if (U[i] >= lo) inner = U[i];
+            }
+            t->fexp_bin[b] = make_float2(inner, __int_as_float(base));
+        }
     }
 }
 
@@ -162,8 +198,8 @@ __device__ __forceinline__ float lse32(const PolyTables* __restrict__ pt, float 
     const float hi = sw ? b : a;
     const float lo = sw ? a : b;
     const float d = __fsub_rn(hi, lo);
-    const int seg = (d >= LSE_T0) + (d >= LSE_T1) + (d >= LSE_T2) + (d >= LSE_T3) +
-                    (d >= LSE_T4) + (d >= LSE_T5) + (d >= LSE_T6);
+    const float2 e = pt->lse_bin[min(__float2int_rz(__fmul_rn(d, 4.0f)), kLseBins - 1)];
+    const int seg = __float_as_int(e.y) + (d >= e.x);
     const float r = cubic(pt->lse[seg], d);
     const float res = __fadd_rn(lo, r);
     return (lo < CF_HALF32 || d >= LSE_TMAX) ? hi : res;
@@ -176,7 +212,9 @@ __device__ __forceinline__ float fexp32(const PolyTables* __restrict__ pt, float
         if (x > (float)46.052) return (float)1e20;
         return (float)exp((double)x);
     }
-    const int seg = (x >= FEXP_T1) + (x >= FEXP_T2) + (x >= FEXP_T3) + (x >= FEXP_T4) + (x >= FEXP_T5);
+    const float u = -x;   // x < 0: x >= T_k  <=>  u <= -T_k
+    const float2 e = pt->fexp_bin[min(__float2int_rz(__fmul_rn(u, 4.0f)), kFexpBins - 1)];
+    const int seg = __float_as_int(e.y) + (u <= e.x);
     const float r = cubic(pt->fexp[seg], x);
     return x < FEXP_T0 ? 0.0f : r;
 }
