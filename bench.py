@@ -369,7 +369,13 @@ def our_arm(args):
                                   "(sm_max_mhz of MEASURED_PEAKS.json); the DP is a log/max semiring, "
                                   "neither HBM- nor tensor-bound",
                      "ops_per_fold": ops_per_fold[dom],
-                     "phase_ms": {names[k]: float(ph[k]) for k in range(4)}},
+                     "phase_ms": {names[k]: float(ph[k]) for k in range(4)},
+                     "hbm": None if traffic is None or not peaks.get("hbm_gbs") else {
+                         "traffic_gbs": traffic / (ph[dom] / 1000.0) / 1e9,
+                         "peak_gbs": float(peaks["hbm_gbs"]),
+                         "frac_of_measured": traffic / (ph[dom] / 1000.0) / 1e9 / float(peaks["hbm_gbs"]),
+                         "note": "ncu DRAM bytes per launch (profiles/ncu_traffic.json) over the measured launch "
+                                 "time: the kernel is not HBM-bound"}},
         "ops_per_fold_total": float(sum(counts[c] * OP_COST[c] for c in range(8))),
         "logz_max_abs_err_fp32_vs_fp64": logz_err,
         "cpu_baseline": cpu,
@@ -396,8 +402,10 @@ def serving_arm(args):
            "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
            "config": {"workload": "serving: Poisson arrivals, lengths log-normal median 150 nt sigma 0.6 clipped 30-1000, "
                                   "40% logZ / 40% MEA / 20% sample x10, 10% masked",
-                      "workers": args.workers, "long_workers": args.long_workers}}
-    with serve.Server(P, workers=args.workers, long_workers=args.long_workers) as srv:
+                      "workers": args.workers, "long_workers": args.long_workers, "long_len": args.long_len,
+                      "edges": args.edges}}
+    with serve.Server(P, workers=args.workers, long_workers=args.long_workers, long_len=args.long_len,
+                      edges=args.edges) as srv:
         warm, _ = serve.mixed_workload(2000, rate=1e9, seed=99)
         srv.replay(warm, np.zeros(len(warm)), keep_results=False)
         n_sat = args.serve_n
@@ -425,6 +433,15 @@ def serving_arm(args):
                 for op in ("logz", "mea", "sample"):
                     sel = np.array([r.op == op for r in reqs])
                     pt[f"p99_{op}_ms"] = round(float(np.percentile(lat[sel], 99)), 3)
+                lens = np.array([len(r.seq) for r in reqs])
+                for lo, hi in ((0, 256), (257, 512), (513, 1000)):
+                    sel = (lens >= lo) & (lens <= hi)
+                    if sel.any():
+                        pt[f"p50_p99_len{lo}-{hi}_ms"] = [round(float(np.percentile(lat[sel], 50)), 1),
+                                                          round(float(np.percentile(lat[sel], 99)), 1)]
+                done = max(1, st1["done"] - st0["done"])
+                pt["mean_wait_ms"] = round(1e3 * (st1["wait_s"] - st0["wait_s"]) / done, 1)
+                pt["mean_batch_run_ms"] = round(1e3 * (st1["serve_s"] - st0["serve_s"]) / done, 1)
                 points.append(pt)
                 if frac == check_frac:
                     check = (reqs, rep.results)
@@ -604,6 +621,9 @@ def main():
                          "logz / sampling / grad: the other measured workloads")
     ap.add_argument("--workers", type=int, default=6, help="serving: engines / worker threads")
     ap.add_argument("--long-workers", type=int, default=2, help="serving: workers that take long requests")
+    ap.add_argument("--long-len", type=int, default=256, help="serving: buckets above this length are long")
+    ap.add_argument("--edges", type=int, nargs="+", default=[96, 192, 256, 384, 640],
+                    help="serving: length-bucket upper edges")
     ap.add_argument("--serve-n", type=int, default=20000, help="serving: requests of the saturation run")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: seconds of arrivals per load point")
     ap.add_argument("--serve-fracs", type=float, nargs="+", default=[0.2, 0.5, 0.8, 0.9])

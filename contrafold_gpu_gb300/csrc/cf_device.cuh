@@ -194,9 +194,10 @@ __device__ __forceinline__ float cubic(const float4 c, float x) {
 
 // log(exp(a) + exp(b)), CONTRAfold Fast_LogPlusEquals (RealT = float).
 __device__ __forceinline__ float lse32(const PolyTables* __restrict__ pt, float a, float b) {
-    const bool sw = a < b;
-    const float hi = sw ? b : a;
-    const float lo = sw ? a : b;
+    // the larger and the smaller argument (the reference swaps on a < b; for
+    // the finite inputs here fmaxf / fminf give the same pair)
+    const float hi = fmaxf(a, b);
+    const float lo = fminf(a, b);
     const float d = __fsub_rn(hi, lo);
     const float2 e = pt->lse_bin[min(__float2int_rz(__fmul_rn(d, 4.0f)), kLseBins - 1)];
     const int seg = __float_as_int(e.y) + (d >= e.x);

@@ -43,13 +43,21 @@ template <typename T>
 struct DevBuf {
     T* p = nullptr;
     size_t cap = 0;   // elements
+    // Grows geometrically (at least doubling): cudaFree waits for the whole
+    // device, so a buffer that is re-sized on every larger batch would stall
+    // every other stream (the serving loop runs several engines at once).
     int ensure(size_t n) {
         if (n <= cap) return CF_OK;
         if (p) cudaFree(p);
         p = nullptr;
+        size_t want = std::max<size_t>(std::max<size_t>(n, 1), 2 * cap);
         cap = 0;
-        size_t want = std::max<size_t>(n, 1);
         cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaErrorMemoryAllocation && want > std::max<size_t>(n, 1)) {   // no room to double
+            cudaGetLastError();
+            want = std::max<size_t>(n, 1);
+            e = cudaMalloc(&p, want * sizeof(T));
+        }
         if (e != cudaSuccess) {
             p = nullptr;
             return fail(CF_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));

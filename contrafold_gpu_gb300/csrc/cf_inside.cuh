@@ -136,6 +136,12 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 #endif
 constexpr int kChainPF = CF_CHAIN_PF;
 constexpr int kChainAsync = CF_CHAIN_ASYNC;
+// CF_CHAIN_UNROLL = 1 unrolls the asynchronous pipeline over its ring slots
+// (constant slot addresses, more code)
+#ifndef CF_CHAIN_UNROLL
+#define CF_CHAIN_UNROLL 0
+#endif
+constexpr bool kChainUnroll = CF_CHAIN_UNROLL != 0;
 
 __device__ __forceinline__ void cp_async_f32(float* smem, const float* gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -169,15 +175,33 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
             if (u < n) issue(u);
             cp_async_commit();
         }
-        int rd = 0, wr = D;   // slots of term k and of term k + D
-        for (int k = 0; k < n; ++k) {
-            cp_async_wait<D - 1>();   // term k has landed
-            const R x = cf_chain_ring[rd][0][tid], y = cf_chain_ring[rd][1][tid];
-            if (k + D < n) issue(wr);
-            cp_async_commit();
-            step(k, x, y);
-            rd = rd + 1 == NS ? 0 : rd + 1;
-            wr = wr + 1 == NS ? 0 : wr + 1;
+        if constexpr (kChainUnroll) {
+            // unrolled over the ring: term k sits in slot k mod NS, term k + D
+            // goes to slot (k + D) mod NS = (k - 1) mod NS -- compile-time slots
+            for (int k0 = 0; k0 < n; k0 += NS) {
+#pragma unroll
+                for (int u = 0; u < NS; ++u) {
+                    const int k = k0 + u;
+                    if (k < n) {
+                        cp_async_wait<D - 1>();   // term k has landed
+                        const R x = cf_chain_ring[u][0][tid], y = cf_chain_ring[u][1][tid];
+                        if (k + D < n) issue((u + D) % NS);
+                        cp_async_commit();
+                        step(k, x, y);
+                    }
+                }
+            }
+        } else {
+            int rd = 0, wr = D;   // slots of term k and of term k + D
+            for (int k = 0; k < n; ++k) {
+                cp_async_wait<D - 1>();   // term k has landed
+                const R x = cf_chain_ring[rd][0][tid], y = cf_chain_ring[rd][1][tid];
+                if (k + D < n) issue(wr);
+                cp_async_commit();
+                step(k, x, y);
+                rd = rd + 1 == NS ? 0 : rd + 1;
+                wr = wr + 1 == NS ? 0 : wr + 1;
+            }
         }
         cp_async_wait<0>();
         return;
@@ -364,6 +388,9 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
     for (int l1 = 0; l1 < nr; ++l1) {
         const int p = i + l1;
         const int qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
+        // the 1-nt bulge and 1x1 terms of this row by l2 = 0, 1 (zero beyond)
+        const R sn0 = l1 == 1 ? P.b01(si1) : R(0);
+        const R sn1 = l1 == 0 ? P.b01(sj) : (l1 == 1 ? P.i11(si1, sj) : R(0));
         uint32_t msk = l1 < nrows ? Q.window(p + 1, qlo, j - qlo + 1) : 0u;
         const int slots = __reduce_max_sync(lanes, __popc(msk));
         lockstep_row<true, R>(
@@ -378,10 +405,7 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
                 } else {
                     const int sq = Q.s[q], sa = Q.s[a];
                     const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
-                    R snuc = R(0);
-                    if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-                    else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-                    else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+                    const R snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : R(0));
                     e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
                 }
                 acc = sr.plus(acc, S::add(e, v));

@@ -232,7 +232,14 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
         const int i = a - 1 - l1;
         return T.FCo[tri_off(j - i, m) + i];
     };
-    auto source = [&](int l1, int j, float v) {
+    // the 1-nt bulge and 1x1 terms of row l1 by l2 = 0, 1 (l2 = 1 is j = b+2)
+    const int sb2 = Q.s[b + 2];
+    auto snuc_row = [&](int l1, float& sn0, float& sn1) {
+        const int si1 = l1 <= l1max ? Q.s[a - l1] : 4;   // rows past this lane's last are empty
+        sn0 = l1 == 1 ? P.b01(si1) : 0.0f;
+        sn1 = l1 == 0 ? P.b01(sb2) : (l1 == 1 ? P.i11(si1, sb2) : 0.0f);
+    };
+    auto source = [&](int l1, int j, float v, float sn0, float sn1) {
         const int i = a - 1 - l1;
         if (!(v > CF_HALF32)) return;
         const int l2 = j - (b + 1);
@@ -242,10 +249,7 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[j + 1], si1, sj));
         } else {
             const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
-            float snuc = 0.0f;
-            if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-            else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-            else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+            const float snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f);
             e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), bp_ab), jBij), jB2), snuc);
         }
         acc = sr.plus(acc, __fadd_rn(v, e));
@@ -259,9 +263,11 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             msk &= ~1u;   // the stacking source comes after the FM1o term
         }
         const int slots = __reduce_max_sync(lanes, __popc(msk));
+        float sn0, sn1;
+        snuc_row(l1, sn0, sn1);
         lockstep_row<true, float>(
             msk, slots, [&](int bit) { return src_val(l1, b + 1 + bit); },
-            [&](int bit, float v) { source(l1, b + 1 + bit, v); });
+            [&](int bit, float v) { source(l1, b + 1 + bit, v, sn0, sn1); });
     }
     if (l1max >= 0) {
         if (b + 1 < L) {
@@ -269,7 +275,7 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             const float jAji = junctionA_rev<Lse32>(P, L, Q, a - 1, b + 1);
             acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(v, jAji), P.mp()), bp_ab));
         }
-        if (m0 & 1u) source(0, b + 1, src_val(0, b + 1));
+        if (m0 & 1u) source(0, b + 1, src_val(0, b + 1), 0.0f, 0.0f);   // stacking: no snuc
     }
     T.FCo[tri_off(t, m) + a] = acc;
 }
@@ -304,7 +310,14 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
         const int i = a - 1 - l1;
         return T.FCo[tri_off(j - i, m) + i];
     };
-    auto source = [&](int l1, int j, float fco) {
+    // the 1-nt bulge and 1x1 terms of row l1 by l2 = 0, 1 (l2 = 1 is j = b+1)
+    const int sb1 = Q.s[b + 1];
+    auto snuc_row = [&](int l1, float& sn0, float& sn1) {
+        const int si1 = l1 <= l1max ? Q.s[a - l1] : 4;   // rows past this lane's last are empty
+        sn0 = l1 == 1 ? P.b01(si1) : 0.0f;
+        sn1 = l1 == 0 ? P.b01(sb1) : (l1 == 1 ? P.i11(si1, sb1) : 0.0f);
+    };
+    auto source = [&](int l1, int j, float fco, float sn0, float sn1) {
         const int i = a - 1 - l1;
         const float outside = __fsub_rn(fco, Z);
         if (!(outside > CF_HALF32)) return;
@@ -315,10 +328,7 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
             e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j + 1], si1, sj)), fcin);
         } else {
             const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
-            float snuc = 0.0f;
-            if (l1 == 0 && l2 == 1) snuc = P.b01(sj);
-            else if (l1 == 1 && l2 == 0) snuc = P.b01(si1);
-            else if (l1 == 1 && l2 == 1) snuc = P.i11(si1, sj);
+            const float snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f);
             e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l1, l2)), fcin), bp_ab), jB2), snuc);
         }
         post = __fadd_rn(post, fexp32(pt, e));
@@ -327,7 +337,7 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
     uint32_t m0 = 0u;
     if (l1max >= 0) {
         m0 = rowmask(0);
-        if (m0 & 1u) source(0, b, src_val(0, b));
+        if (m0 & 1u) source(0, b, src_val(0, b), 0.0f, 0.0f);   // stacking: no snuc
         if (b < L) {
             const float v = T.FM1o[tri_off(b - a + 1, m) + a - 1];
             if (v > CF_HALF32) {
@@ -342,9 +352,11 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
     for (int l1 = 0; l1 <= lm; ++l1) {
         uint32_t msk = l1 == 0 ? m0 : (l1 <= l1max ? rowmask(l1) : 0u);
         const int slots = __reduce_max_sync(lanes, __popc(msk));
+        float sn0, sn1;
+        snuc_row(l1, sn0, sn1);
         lockstep_row<false, float>(
             msk, slots, [&](int bit) { return src_val(l1, b + bit); },
-            [&](int bit, float v) { source(l1, b + bit, v); });
+            [&](int bit, float v) { source(l1, b + bit, v, sn0, sn1); });
     }
     if (!live) return 0.0f;
     const float outside = __fsub_rn(T.F5o[b], Z);

@@ -55,7 +55,7 @@ struct Req {
     std::string err;
     float logz = 0.f;
     std::string out;           // dot-bracket (MEA) or n_samples * L bytes (sampling)
-    Clock::time_point t_submit, t_done;
+    Clock::time_point t_submit, t_start, t_done;
 };
 
 struct Key {
@@ -94,6 +94,8 @@ struct cf_server {
     // statistics
     int64_t n_batches = 0, n_done = 0, nt_done = 0, n_cancelled = 0;
     double busy_s = 0;                   // summed batch wall time over workers
+    double wait_s = 0, max_wait_s = 0;   // queue wait (submit -> batch start) over requests
+    double serve_s = 0, max_serve_s = 0; // batch run time seen by each request
 
     int bucket_of(int32_t L) const {
         int b = 0;
@@ -201,14 +203,21 @@ void worker_loop(cf_server* S, int w) {
             if (S->queued > 0) S->cv_work.notify_all();
         }
         const auto t0 = Clock::now();
+        for (Req* r : batch) r->t_start = t0;
         run_batch(S, eng, key, batch, buf, offs, mask, seeds, lz, out);
         const auto t1 = Clock::now();
         {
             std::lock_guard<std::mutex> lk(S->mu);
+            const double serve = std::chrono::duration<double>(t1 - t0).count();
             for (Req* r : batch) {
                 r->state = kDone;
                 r->t_done = t1;
                 S->nt_done += (int64_t)r->seq.size();
+                const double wait = std::chrono::duration<double>(t0 - r->t_submit).count();
+                S->wait_s += wait;
+                S->max_wait_s = std::max(S->max_wait_s, wait);
+                S->serve_s += serve;
+                S->max_serve_s = std::max(S->max_serve_s, serve);
             }
             S->n_done += (int64_t)batch.size();
             S->n_batches += 1;
@@ -449,7 +458,7 @@ int cf_server_stats(cf_server* S, double* stats, int32_t n_stats) {
     if (!S || !stats) return fail(CF_EINVAL, "NULL argument");
     std::lock_guard<std::mutex> lk(S->mu);
     const double v[] = {(double)S->n_batches, (double)S->n_done, (double)S->nt_done, (double)S->n_cancelled,
-                        S->busy_s, (double)S->queued};
+                        S->busy_s, (double)S->queued, S->wait_s, S->max_wait_s, S->serve_s, S->max_serve_s};
     for (int k = 0; k < n_stats && k < (int)(sizeof v / sizeof v[0]); ++k) stats[k] = v[k];
     return CF_OK;
 }

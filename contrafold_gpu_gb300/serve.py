@@ -165,10 +165,11 @@ class Server:
         self._check(self.lib.cf_server_cancel(self._h, ticket))
 
     def stats(self) -> dict:
-        v = np.zeros(6)
-        self._check(self.lib.cf_server_stats(self._h, _p(v, ctypes.c_double), 6))
+        v = np.zeros(10)
+        self._check(self.lib.cf_server_stats(self._h, _p(v, ctypes.c_double), 10))
         return dict(batches=int(v[0]), done=int(v[1]), nucleotides=int(v[2]), cancelled=int(v[3]),
-                    busy_s=float(v[4]), queued=int(v[5]))
+                    busy_s=float(v[4]), queued=int(v[5]), wait_s=float(v[6]), max_wait_s=float(v[7]),
+                    serve_s=float(v[8]), max_serve_s=float(v[9]))
 
     def replay(self, requests: Sequence[Request], arrivals: Sequence[float], keep_results: bool = True) -> ReplayResult:
         """Open-loop replay: request k is submitted arrivals[k] seconds after the

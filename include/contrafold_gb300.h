@@ -247,8 +247,10 @@ int cf_server_replay(cf_server* server, int32_t n, const double* t_arrive,
                      const cf_request* reqs, const uint8_t* seqs, const int64_t* offsets,
                      const uint8_t* mask, const int64_t* out_offsets, float* logz_out,
                      char* out, double* latency_ms, int32_t* status_out);
-/* stats[0..5] = batches, requests done, nucleotides done, cancelled,
- * summed batch seconds over workers, requests queued now. */
+/* stats[0..9] = batches, requests done, nucleotides done, cancelled,
+ * summed batch seconds over workers, requests queued now, summed and maximum
+ * queue wait (submit to batch start, seconds) over done requests, summed and
+ * maximum batch run time seen by a request (seconds). */
 int cf_server_stats(cf_server* server, double* stats, int32_t n_stats);
 
 /* ---- MEA without device allocation ----
