@@ -289,9 +289,13 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");
     const void* ks[] = {(const void*)cf::k_plain_inside32, (const void*)cf::k_plain_outside32,
                         (const void*)cf::k_plain_posterior32, (const void*)cf::k_plain_mea32,
-                        (const void*)cf::k_inside32, (const void*)cf::k_inside32acc, (const void*)cf::k_inside64, (const void*)cf::k_outside32,
-                        (const void*)cf::k_posterior32, (const void*)cf::k_mea32, (const void*)cf::k_viterbi64};
+                        (const void*)cf::k_inside64, (const void*)cf::k_viterbi64};
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (bool wide : {false, true}) {
+        const cf::FoldKernels fk = cf::fold_kernels(wide);
+        for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea})
+            CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    }
     for (int mode = 0; mode < 4; ++mode)
         CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (int mode = 0; mode < 3; ++mode)
@@ -462,9 +466,18 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         A.status = X.status;
         const int grid = (A.n + P.group - 1) / P.group;
         const dim3 blk(cf::kFoldThreads);
+        // at most one CTA per SM: the wide per-phase kernels (twice the threads on
+        // each diagonal, the latency of small batches of long sequences)
+        int sms = 0;
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        const bool wide = grid <= sms;
+        const dim3 blkw(wide ? cf::kFoldThreadsWide : cf::kFoldThreads);
+        const cf::FoldKernels fk = cf::fold_kernels(wide);
+        const cf::FoldKernel k_in = fk.inside, k_inacc = fk.inside_acc, k_out = fk.outside, k_post = fk.posterior,
+                             k_dec = fk.mea;
         switch (job) {
             case JOB_LOGZ:
-                CF_PHASE(0, (cf::k_inside32acc<<<grid, blk, smem, st>>>(A)));
+                CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
                 break;
             case JOB_LOGZ64:
                 CF_PHASE(0, (cf::k_inside64<<<grid, blk, smem, st>>>(A)));
@@ -488,16 +501,16 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                     }
                     break;
                 }
-                CF_PHASE(0, (cf::k_inside32<<<grid, blk, smem, st>>>(Ai)));
-                CF_PHASE(1, (cf::k_outside32<<<grid, blk, smem, st>>>(A)));
+                CF_PHASE(0, (k_in<<<grid, blkw, smem, st>>>(Ai)));
+                CF_PHASE(1, (k_out<<<grid, blkw, smem, st>>>(A)));
                 if (job == JOB_BPP) {
-                    CF_PHASE(2, (cf::k_posterior32<<<grid, blk, smem, st>>>(A)));
+                    CF_PHASE(2, (k_post<<<grid, blkw, smem, st>>>(A)));
                 } else {
                     cf::FoldArgs Ap = A;
                     Ap.post_out = nullptr;
                     Ap.logz = nullptr;
-                    CF_PHASE(2, (cf::k_posterior32<<<grid, blk, smem, st>>>(Ap)));
-                    CF_PHASE(3, (cf::k_mea32<<<grid, blk, smem, st>>>(A)));
+                    CF_PHASE(2, (k_post<<<grid, blkw, smem, st>>>(Ap)));
+                    CF_PHASE(3, (k_dec<<<grid, blkw, smem, st>>>(A)));
                 }
                 break;
             }
@@ -505,7 +518,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                 CF_PHASE(0, (cf::k_viterbi64<<<grid, blk, smem, st>>>(A)));
                 break;
             case JOB_SAMPLE: {
-                CF_PHASE(0, (cf::k_inside32acc<<<grid, blk, smem, st>>>(A)));
+                CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
                 if (!sj || sj->n_samples <= 0) break;
                 cf::SampleArgs S;
                 S.descs = A.descs;

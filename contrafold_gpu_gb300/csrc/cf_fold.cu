@@ -229,7 +229,8 @@ __device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, con
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside32(FoldArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_inside32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -240,7 +241,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside32(FoldA
 }
 
 // Same recurrence with accurate float32 log-sum-exp: logZ_batch and the sampler.
-__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside32acc(FoldArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_inside32acc(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -328,14 +330,16 @@ __device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldA
         }
 }
 
-__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_outside32(FoldArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_outside32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
     outside_group(sm, A);
 }
 
-__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_posterior32(FoldArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_posterior32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -400,7 +404,8 @@ __device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A
 
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
 // with the reference's strict-'>' candidate order, BFS traceback.
-__global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_mea32(FoldArgs A) {
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_mea32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);
@@ -625,6 +630,25 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_viterbi64(Fold
 }
 
 // ---------------------------------------------------------------------------
+template __global__ void k_inside32<kFoldThreads>(FoldArgs);
+template __global__ void k_inside32<kFoldThreadsWide>(FoldArgs);
+template __global__ void k_inside32acc<kFoldThreads>(FoldArgs);
+template __global__ void k_inside32acc<kFoldThreadsWide>(FoldArgs);
+template __global__ void k_outside32<kFoldThreads>(FoldArgs);
+template __global__ void k_outside32<kFoldThreadsWide>(FoldArgs);
+template __global__ void k_posterior32<kFoldThreads>(FoldArgs);
+template __global__ void k_posterior32<kFoldThreadsWide>(FoldArgs);
+template __global__ void k_mea32<kFoldThreads>(FoldArgs);
+template __global__ void k_mea32<kFoldThreadsWide>(FoldArgs);
+
+FoldKernels fold_kernels(bool wide) {
+    if (wide)
+        return {k_inside32<kFoldThreadsWide>, k_inside32acc<kFoldThreadsWide>, k_outside32<kFoldThreadsWide>,
+                k_posterior32<kFoldThreadsWide>, k_mea32<kFoldThreadsWide>};
+    return {k_inside32<kFoldThreads>, k_inside32acc<kFoldThreads>, k_outside32<kFoldThreads>,
+            k_posterior32<kFoldThreads>, k_mea32<kFoldThreads>};
+}
+
 size_t fold_smem_bytes(int Lmax, int group, bool fp64) {
     const size_t head = fp64 ? sizeof(SmemFold<double>) : sizeof(SmemFold<float>);
     return head + 2 * (size_t)code_stride(Lmax) * group + (size_t)group * 4 * pb_words(Lmax) * 4;

@@ -8,8 +8,10 @@
 
 namespace cf {
 
-constexpr int kFoldThreads = 256;   // threads per fold CTA
-constexpr int kFoldMinBlocks = 3;   // resident CTAs per SM the register budget targets
+constexpr int kFoldThreads = 256;       // threads per fold CTA
+constexpr int kFoldMinBlocks = 3;       // resident CTAs per SM the register budget targets
+constexpr int kFoldThreadsWide = 512;   // per-phase fold CTA when the grid has at most one CTA per SM:
+                                        // a long sequence's diagonal spreads over twice the threads
 constexpr int kMaxGroup = 32;       // sequences per CTA on the batched path
 
 struct FoldArgs {
@@ -30,12 +32,15 @@ struct FoldArgs {
     int* status;               // device status word (CF_OK or an error code)
 };
 
-__global__ void k_inside32(FoldArgs A);
-__global__ void k_inside32acc(FoldArgs A);
+// FP32 per-phase kernels (k_inside32, k_inside32acc, k_outside32,
+// k_posterior32, k_mea32), instantiated for kFoldThreads and kFoldThreadsWide
+// threads per CTA in cf_fold.cu and reached through fold_kernels().
+using FoldKernel = void (*)(FoldArgs);
+struct FoldKernels {
+    FoldKernel inside, inside_acc, outside, posterior, mea;
+};
+FoldKernels fold_kernels(bool wide);
 __global__ void k_inside64(FoldArgs A);
-__global__ void k_outside32(FoldArgs A);
-__global__ void k_posterior32(FoldArgs A);
-__global__ void k_mea32(FoldArgs A);
 __global__ void k_viterbi64(FoldArgs A);
 
 size_t fold_smem_bytes(int Lmax, int group, bool fp64);
