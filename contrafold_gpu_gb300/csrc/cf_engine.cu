@@ -188,7 +188,14 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // sequences per SM in flight (their tables stay in L2); the warp kernel
     // runs one sequence per warp (short sequences, sampling).
     int sched = eng->sched;
-    if (sched == 0) sched = (P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch()) ? 1 : 3;   // 3: grouped
+    // sampling never takes the warp kernel on its own: it draws a sequence's
+    // samples one after another on one warp, the grouped path gives every
+    // (sequence, sample) its own warp (1.28M vs 0.72M samples/s on 40-400 nt).
+    // Mixed lengths stay one plan, longest first: splitting a 40-400 nt batch
+    // at 256 nt into a warp-kernel part and a grouped part on two streams was
+    // slower for every job (MEA 8.5k vs 10.7k folds/s).
+    if (sched == 0)
+        sched = (job != JOB_SAMPLE && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch()) ? 1 : 3;   // 3: grouped
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;

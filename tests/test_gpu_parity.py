@@ -184,3 +184,24 @@ def test_long_sequence_budget_slicing(engine, P, oracle):
         engine.set_budget(0)
     assert full == sliced
     assert full == oracle.batch(oracle.JOB_MEA, seqs, P, masks, 6.0)
+
+
+def test_mixed_lengths_every_schedule(engine):
+    """A batch mixing 20-250 nt with 257-420 nt sequences gives identical results
+    on every schedule (the warp kernel then folds long sequences too)."""
+    from contrafold_gpu_gb300.engine import Batch
+    s1, m1 = _rand_batch(41, 40, 20, 250, 0.1)
+    s2, m2 = _rand_batch(42, 12, 257, 420, 0.1)
+    order = np.random.default_rng(43).permutation(len(s1) + len(s2))
+    seqs = [(s1 + s2)[k] for k in order]
+    masks = [(m1 + m2)[k] for k in order]
+    B = Batch(seqs, masks)
+    res = {}
+    for path in ("auto",) + tuple(PATHS):
+        set_path(engine, path)
+        mats, zb = engine.bpp(B)
+        res[path] = (engine.logz(B).tobytes(), engine.logz64(B).tobytes(), engine.mea(B, 6.0), engine.mfe(B),
+                     zb.tobytes(), hashlib.sha256(np.concatenate([m.ravel() for m in mats]).tobytes()).hexdigest(),
+                     engine.sample(B, 4, seeds=list(range(len(seqs)))))
+    for path in PATHS:
+        assert res[path] == res["auto"], path
