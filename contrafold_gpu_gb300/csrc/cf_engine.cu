@@ -854,7 +854,35 @@ struct cf_plan {
     DevBuf<int> status;
     PhaseTimer timer;
     int launches = 0;
+    // CUDA graph of the plan's launches, replayed while the run arguments stay
+    // the same (cf_plan_set_graph)
+    bool graph_on = false;
+    cudaGraphExec_t gexec = nullptr;
+    const void* g_seqs = nullptr;
+    const void* g_mask = nullptr;
+    void* g_out = nullptr;
+    float g_gamma = 0.f;
+    int g_launches = 0;
 };
+
+namespace {
+
+// Shared memory run_device will ask for: set before a stream capture, which
+// then records kernel launches only.
+int plan_prepare_smem(cf_engine* e, Job job, const Plan& P) {
+    size_t bytes;
+    if (P.cta) {
+        bytes = cf::fold_smem_bytes(P.Lmax, 1, false);
+    } else if (P.warp) {
+        bytes = cf::warp_smem_bytes(P.Lmax);
+    } else {
+        const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
+        bytes = std::max(cf::fold_smem_bytes(P.Lmax, P.group, fp64), cf::plain_smem_bytes(P.Lmax));
+    }
+    return ensure_smem(e, bytes);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -892,6 +920,7 @@ int cf_plan_destroy(cf_plan* p) {
     if (!p) return CF_OK;
     cudaSetDevice(p->eng->device);
     cudaDeviceSynchronize();
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
     p->descs.release(); p->arena.release(); p->status.release();
     delete p;
     return CF_OK;
@@ -912,9 +941,50 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
     float* lz = p->job == JOB_LOGZ ? static_cast<float*>(d_out) : nullptr;
     double* lz64 = p->job == JOB_LOGZ64 ? static_cast<double*>(d_out) : nullptr;
     char* st_out = (p->job == JOB_MEA || p->job == JOB_MFE) ? static_cast<char*>(d_out) : nullptr;
+    if (p->graph_on && !p->timer.on && p->n > 0) {
+        const bool hit = p->gexec != nullptr && p->g_seqs == d_seqs && p->g_mask == d_mask && p->g_out == d_out &&
+                         p->g_gamma == gamma;
+        if (!hit) {   // (re)capture the launches of one run
+            int rc = plan_prepare_smem(p->eng, p->job, p->P);
+            if (rc) return rc;
+            if (p->gexec) {
+                CF_CUDA(cudaGraphExecDestroy(p->gexec));
+                p->gexec = nullptr;
+            }
+            CF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            X.timer = nullptr;
+            rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(st, &g);
+            if (rc || ec != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return rc ? rc : fail(CF_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&p->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                p->gexec = nullptr;
+                return fail(CF_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ei));
+            }
+            p->g_seqs = d_seqs;
+            p->g_mask = d_mask;
+            p->g_out = d_out;
+            p->g_gamma = gamma;
+            p->g_launches = X.launches;
+        }
+        CF_CUDA(cudaGraphLaunch(p->gexec, st));
+        p->launches = p->g_launches;
+        return CF_OK;
+    }
     int rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
     p->launches = X.launches;
     return rc;
+}
+
+int cf_plan_set_graph(cf_plan* p, int on) {
+    if (!p) return fail(CF_EINVAL, "plan is NULL");
+    p->graph_on = on != 0;
+    return CF_OK;
 }
 
 int cf_plan_status(cf_plan* p) {

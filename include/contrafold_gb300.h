@@ -189,6 +189,12 @@ int cf_plan_set_timing(cf_plan* plan, int on);
 int cf_plan_phase_ms(cf_plan* plan, float* ms, int32_t nphases);
 /* Kernels launched by the last cf_plan_run; sequences per CTA of the plan. */
 int cf_plan_launches(const cf_plan* plan);
+/* CUDA graph replay (no reference counterpart): with on != 0, cf_plan_run
+ * records the plan's launches into a CUDA graph by stream capture the first
+ * time it sees a (d_seqs, d_mask, gamma, d_out) combination, and afterwards
+ * launches that graph -- one launch call for all the plan's kernels and
+ * memsets.  New arguments re-capture.  Ignored while phase timing is on. */
+int cf_plan_set_graph(cf_plan* plan, int on);
 int cf_plan_group(const cf_plan* plan);
 
 /* ---- serving loop: continuous batching of single-sequence requests ----
