@@ -9,6 +9,7 @@ speed differs.  The engine's built-in length table (cf_engine.cu,
 auto_warp_max_len / auto_ctas_per_sm) is set from these measurements.
 
     python -m contrafold_gpu_gb300.autotune [--lengths 50,100,200,300,400] [--json out.json]
+    python -m contrafold_gpu_gb300.autotune --lengths 100,200 --batch-sizes 256,1024,4096
 """
 from __future__ import annotations
 
@@ -62,9 +63,24 @@ def main():
     ap.add_argument("--folds", type=float, default=2.5e10, help="work per bucket ~ folds * L^3 (sizes n)")
     ap.add_argument("--job", default="mea", choices=["mea", "logz"])
     ap.add_argument("--json", default=None)
+    ap.add_argument("--batch-sizes", default=None,
+                    help="comma list: time the warp and grouped schedules at each (length, batch size) -- the "
+                         "batch size from which the engine takes the warp kernel (auto_warp_min_batch)")
     args = ap.parse_args()
     from . import load
     P = load()
+    if args.batch_sizes:
+        table = {}
+        for L in [int(x) for x in args.lengths.split(",")]:
+            for n in [int(x) for x in args.batch_sizes.split(",")]:
+                row = {k: time_schedule(P, L, n, k, 0, job=args.job) for k in ("warp", "group")}
+                table[f"{L}x{n}"] = row
+                print(f"L={L:4d} n={n:6d} warp {row['warp']:10.1f} group {row['group']:10.1f} folds/s "
+                      f"-> {'warp' if row['warp'] > row['group'] else 'group'}", flush=True)
+        if args.json:
+            with open(args.json, "w") as fh:
+                json.dump(table, fh, indent=1)
+        return table
     schedules = [("plain", 0), ("warp", 0), ("group", 0), ("cta", 3), ("cta", 4)]
     table = {}
     for L in [int(x) for x in args.lengths.split(",")]:

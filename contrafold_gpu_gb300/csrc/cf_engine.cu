@@ -116,13 +116,15 @@ namespace {
 
 // ---- group-size autotune table: sequences per CTA by length range ----
 // Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
-// Batched-path schedule (GB300 tuning): batches of at least
-// auto_warp_min_batch() sequences, none longer than auto_warp_max_len(), take
-// the warp-per-sequence kernel (throughput); smaller batches fold one sequence
-// per CTA (latency: a single 250-nt MEA fold takes 56 ms on a CTA, 232 ms on a
-// warp).
+// Batched-path schedule (GB300 tuning, autotune.py --batch-sizes): batches of
+// at least auto_warp_min_batch() sequences, none longer than
+// auto_warp_max_len(), take the warp-per-sequence kernel (throughput); smaller
+// batches fold one sequence per CTA (latency: a single 250-nt MEA fold takes
+// 56 ms on a CTA, 232 ms on a warp).  Measured crossover (MEA folds/s, warp vs
+// grouped): 200 nt n=1024 8.7k vs 10.2k, n=2048 15.1k vs 13.3k; 60 nt n=2048
+// 172k vs 186k, n=4096 238k vs 191k.
 int auto_warp_max_len() { return 256; }
-int auto_warp_min_batch() { return 1024; }
+int auto_warp_min_batch(int Lmax) { return Lmax <= 80 ? 4096 : 2048; }
 // CTAs per SM of the persistent CTA kernel by length.
 int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
 
@@ -195,7 +197,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // at 256 nt into a warp-kernel part and a grouped part on two streams was
     // slower for every job (MEA 8.5k vs 10.7k folds/s).
     if (sched == 0)
-        sched = (job != JOB_SAMPLE && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch()) ? 1 : 3;   // 3: grouped
+        sched = (job != JOB_SAMPLE && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch(P.Lmax)) ? 1 : 3;
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;

@@ -94,7 +94,8 @@ int cf_engine_set_mode(cf_engine* eng, int mode);
 /* Batched-path schedule (the tuner's knob): kind 0 = automatic by length,
  * 1 = persistent warp-per-sequence kernel, 2 = persistent CTA-per-sequence
  * fused kernel, 3 = length-grouped per-phase kernels (kind 0 takes the warp
- * kernel for batches of >= 1024 sequences of <= 256 nt, else kind 3); ctas_per_sm caps the
+ * kernel for batches of >= 2048 sequences of <= 256 nt -- 4096 up to 80 nt --
+ * except for sampling, else kind 3); ctas_per_sm caps the
  * persistent CTA kernel's residency (0 = automatic).  Results are identical
  * for every choice. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
