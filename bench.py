@@ -35,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -42,8 +43,7 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-with open(os.path.join(REPO, "BASELINE.json")) as _fh:
-    METRIC = json.load(_fh)["metric"]
+METRIC = "200-nt MEA folds/s, batched vs plain on 1 GB300 at logZ≤5e-4; served p50/p99 ms"
 UNIT = "folds/s"
 
 
@@ -70,7 +70,7 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_dev{device}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"cf_bench_clocks_dev{device}_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
