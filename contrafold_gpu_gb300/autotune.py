@@ -28,7 +28,7 @@ def _batch_bytes(n, L, seed):
     return seq, mask
 
 
-def time_schedule(P, L, n, kind, ctas, reps=3, job="mea"):
+def time_schedule(P, L, n, kind, ctas, reps=3, job="mea", group=0):
     import torch
     from .engine import CF_JOB_LOGZ, CF_JOB_MEA, Engine, Plan
     seq, mask = _batch_bytes(n, L, 7)
@@ -39,6 +39,8 @@ def time_schedule(P, L, n, kind, ctas, reps=3, job="mea"):
     eng = Engine(P, mode="plain" if kind == "plain" else "batched")
     if kind != "plain":
         eng.set_schedule(kind, ctas)
+    if group:
+        eng.set_group(group)
     plan = Plan(eng, CF_JOB_MEA if job == "mea" else CF_JOB_LOGZ, np.arange(n + 1, dtype=np.int64) * L)
     stream = torch.cuda.Stream(dev)
     plan.run(d_seq.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
@@ -66,9 +68,25 @@ def main():
     ap.add_argument("--batch-sizes", default=None,
                     help="comma list: time the warp and grouped schedules at each (length, batch size) -- the "
                          "batch size from which the engine takes the warp kernel (auto_warp_min_batch)")
+    ap.add_argument("--groups", default=None,
+                    help="comma list: time the grouped schedule with each number of sequences per CTA at every "
+                         "length (batch sized as for the schedule table) -- the engine's group_for_length table")
     args = ap.parse_args()
     from . import load
     P = load()
+    if args.groups:
+        table = {}
+        for L in [int(x) for x in args.lengths.split(",")]:
+            n = int(max(304, min(20000, args.folds / L ** 3)))
+            row = {g: time_schedule(P, L, n, "group", 0, job=args.job, group=int(g)) for g in args.groups.split(",")}
+            best = max(row, key=row.get)
+            table[L] = {"n": n, "folds_per_s": row, "best": int(best)}
+            print(f"L={L:4d} n={n:6d} " + " ".join(f"g{g}:{v:9.1f}" for g, v in row.items()) + f" -> group {best}",
+                  flush=True)
+        if args.json:
+            with open(args.json, "w") as fh:
+                json.dump(table, fh, indent=1)
+        return table
     if args.batch_sizes:
         table = {}
         for L in [int(x) for x in args.lengths.split(",")]:

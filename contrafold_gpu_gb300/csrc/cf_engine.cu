@@ -109,6 +109,7 @@ struct cf_engine {
     int mode = 1;        // 0 plain, 1 batched
     int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent
     int ctas_per_sm = 0; // CTA-persistent occupancy cap (0 = auto)
+    int group = 0;       // sequences per CTA of the grouped kernels (0 = auto)
     size_t smem_optin = 0;
 };
 
@@ -163,13 +164,22 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
             return offsets[x + 1] - offsets[x] > offsets[y + 1] - offsets[y];
         });
-        // one group size for the launch: that of the median length, but only as
-        // many sequences per CTA as still leave two CTAs per SM
+        // one group size for the launch (GB300, autotune.py --groups and batch
+        // policies): lengths within 25 % of each other fold best as ONE wave of
+        // CTAs (kFoldMinBlocks per SM) each holding n / slots sequences (200 nt:
+        // n=1000 9.9k -> 14.4k, n=3125 15.0k -> 23.9k MEA folds/s against two
+        // per CTA); mixed lengths keep several waves so the long sequences' CTAs
+        // do not set the end alone (40-400 nt: 11.8k with 2 per CTA, 6.5k with 9)
         const int Lmed = n ? (int)(offsets[order[n / 2] + 1] - offsets[order[n / 2]]) : 0;
+        const int Lmin = n ? (int)(offsets[order[n - 1] + 1] - offsets[order[n - 1]]) : 0;
         int sms = 0;
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
-        const int fill = std::max(1, n / std::max(1, 2 * sms));
-        P.group = std::min(std::min(cf::kMaxGroup, group_for_length(Lmed)), fill);
+        const int slots = std::max(1, cf::kFoldMinBlocks * sms);
+        const int wave1 = std::min(cf::kMaxGroup, std::max(1, (n + slots - 1) / slots));
+        const int wave2 = std::min(cf::kMaxGroup, std::max(1, (n + 2 * slots - 1) / (2 * slots)));
+        const bool uniform = P.Lmax <= Lmin + Lmin / 4;
+        P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group)
+                                 : uniform ? wave1 : std::min(group_for_length(Lmed), wave2);
     }
     for (int k = 0; k < n; ++k) {
         const int b = order[k];
@@ -728,6 +738,13 @@ int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
     if (kind < 0 || kind > 3 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
     e->sched = kind;
     e->ctas_per_sm = ctas_per_sm;
+    return CF_OK;
+}
+
+int cf_engine_set_group(cf_engine* e, int group) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    if (group < 0 || group > cf::kMaxGroup) return fail(CF_EINVAL, "group must be in [0, 32]");
+    e->group = group;
     return CF_OK;
 }
 

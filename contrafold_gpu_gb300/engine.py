@@ -24,7 +24,7 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
+           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group", "cf_plan_set_graph", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
@@ -60,6 +60,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_engine_set_budget.argtypes = [vp, ctypes.c_size_t]
         L.cf_engine_set_mode.argtypes = [vp, ctypes.c_int]
         L.cf_engine_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        L.cf_engine_set_group.argtypes = [vp, ctypes.c_int]
         L.cf_last_error.restype = ctypes.c_char_p
         L.cf_version.restype = ctypes.c_char_p
         L.cf_logz.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f32p]
@@ -83,7 +84,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_group.argtypes = [vp]
         L.cf_plan_set_graph.argtypes = [vp, ctypes.c_int]
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
+                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
                      "cf_sample_seeded", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group", "cf_plan_set_graph"):
             getattr(L, name).restype = ctypes.c_int
@@ -174,6 +175,10 @@ class Engine:
         """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap) or 'group'."""
         self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3}[kind],
                                                     int(ctas_per_sm)))
+
+    def set_group(self, group: int = 0):
+        """Sequences per CTA of the grouped kernels (0 = automatic)."""
+        self._check(self.lib.cf_engine_set_group(self._h, int(group)))
 
     def set_budget(self, nbytes: int):
         self._check(self.lib.cf_engine_set_budget(self._h, int(nbytes)))

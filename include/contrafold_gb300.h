@@ -99,6 +99,10 @@ int cf_engine_set_mode(cf_engine* eng, int mode);
  * persistent CTA kernel's residency (0 = automatic).  Results are identical
  * for every choice. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
+/* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32, or
+ * 0 = automatic (by the median length, capped to keep two CTAs per SM).  The
+ * tuner's knob; results are identical for every value. */
+int cf_engine_set_group(cf_engine* eng, int group);
 
 const char* cf_last_error(void);
 const char* cf_version(void);

@@ -205,3 +205,18 @@ def test_mixed_lengths_every_schedule(engine):
                      engine.sample(B, 4, seeds=list(range(len(seqs)))))
     for path in PATHS:
         assert res[path] == res["auto"], path
+
+
+def test_long_sequence_vs_oracle(engine, P, oracle):
+    """One 600-nt sequence (10 % mask): 512-thread per-phase kernels with several
+    cells per thread on each diagonal; Viterbi and MEA identical, BPP bitwise,
+    FP64 logZ to 1e-9 relative."""
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(61, 1, 600, 600, 0.1)
+    B = Batch(seqs, masks)
+    assert engine.mfe(B)[0] == oracle.mfe(seqs[0], P, masks[0])
+    assert engine.mea(B, 6.0)[0] == oracle.mea(seqs[0], P, 6.0, masks[0])
+    z64 = oracle.logz64(seqs[0], P, masks[0])
+    assert abs(engine.logz64(B)[0] - z64) <= 1e-9 * abs(z64)
+    # float32 logZ: the 5e-4 of the 200-nt contract, scaled with the length (600 / 200)
+    assert abs(engine.logz(B)[0] - z64) <= 5e-4 * 3
