@@ -157,7 +157,16 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     std::iota(order.begin(), order.end(), 0);
     P.group = 1;
     P.Lmax = 0;
-    for (int b = 0; b < n; ++b) P.Lmax = std::max<int>(P.Lmax, (int)(offsets[b + 1] - offsets[b]));
+    int Lmin = n ? CF_MAX_LEN : 0;
+    for (int b = 0; b < n; ++b) {
+        P.Lmax = std::max<int>(P.Lmax, (int)(offsets[b + 1] - offsets[b]));
+        Lmin = std::min<int>(Lmin, (int)(offsets[b + 1] - offsets[b]));
+    }
+    // lengths within 25 % of each other: the grouped kernels with whole waves
+    // of full CTAs beat the warp kernel (10,000 x 200 nt MEA: 27.7k vs 25.2k
+    // folds/s; 10,000 x 100 nt: 121k vs 109k); mixed lengths keep the warp
+    // kernel's per-sequence work queue (150-250 nt: 20.8k vs 15.1k)
+    const bool uniform = P.Lmax <= Lmin + Lmin / 4;
     const bool batched = eng->mode == 1 && job != JOB_GRAD;
     P.plain = !batched;
     if (batched) {
@@ -171,15 +180,15 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         // per CTA); mixed lengths keep several waves so the long sequences' CTAs
         // do not set the end alone (40-400 nt: 11.8k with 2 per CTA, 6.5k with 9)
         const int Lmed = n ? (int)(offsets[order[n / 2] + 1] - offsets[order[n / 2]]) : 0;
-        const int Lmin = n ? (int)(offsets[order[n - 1] + 1] - offsets[order[n - 1]]) : 0;
         int sms = 0;
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
         const int slots = std::max(1, cf::kFoldMinBlocks * sms);
-        const int wave1 = std::min(cf::kMaxGroup, std::max(1, (n + slots - 1) / slots));
+        // whole waves: the fewest waves whose groups fit kMaxGroup sequences
+        const int waves = std::max(1, (n + cf::kMaxGroup * slots - 1) / (cf::kMaxGroup * slots));
+        const int wave_group = std::min(cf::kMaxGroup, std::max(1, (n + waves * slots - 1) / (waves * slots)));
         const int wave2 = std::min(cf::kMaxGroup, std::max(1, (n + 2 * slots - 1) / (2 * slots)));
-        const bool uniform = P.Lmax <= Lmin + Lmin / 4;
         P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group)
-                                 : uniform ? wave1 : std::min(group_for_length(Lmed), wave2);
+                                 : uniform ? wave_group : std::min(group_for_length(Lmed), wave2);
     }
     for (int k = 0; k < n; ++k) {
         const int b = order[k];
@@ -207,7 +216,8 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // at 256 nt into a warp-kernel part and a grouped part on two streams was
     // slower for every job (MEA 8.5k vs 10.7k folds/s).
     if (sched == 0)
-        sched = (job != JOB_SAMPLE && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch(P.Lmax)) ? 1 : 3;
+        sched = (job != JOB_SAMPLE && !uniform && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch(P.Lmax))
+                    ? 1 : 3;
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
