@@ -9,7 +9,10 @@
 namespace cf {
 
 constexpr int kFoldThreads = 256;       // threads per fold CTA
-constexpr int kFoldMinBlocks = 3;       // resident CTAs per SM the register budget targets
+#ifndef CF_FOLD_MIN_BLOCKS
+#define CF_FOLD_MIN_BLOCKS 3
+#endif
+constexpr int kFoldMinBlocks = CF_FOLD_MIN_BLOCKS;   // resident CTAs per SM the register budget targets
 constexpr int kFoldThreadsWide = 512;   // per-phase fold CTA when the grid has at most one CTA per SM:
                                         // a long sequence's diagonal spreads over twice the threads
 constexpr int kMaxGroup = 32;       // sequences per CTA on the batched path
