@@ -28,6 +28,7 @@ struct SmemFold {
     int n;        // sequences in this group
     int gcap;     // sequences per CTA of the launch (sizes the dynamic region)
     int Lmax;
+    int step_ctr[2];   // per-step work counters of step_items (by step parity)
 };
 
 __host__ __device__ __forceinline__ int code_stride(int Lmax) { return (Lmax + 2 + 15) & ~15; }
@@ -145,9 +146,21 @@ __device__ __forceinline__ PairList plist_of(const FoldArgs& A, int64_t ws_off, 
 // diagonal dB, from the pair lists) then phase-A items (every cell of
 // diagonal dA).  The B block is padded to a multiple of 32 so that each warp
 // holds one kind of item.  fB(g, i), fA(g, i) process one cell.
+//
+// Warps claim 32-item chunks from a shared counter (B chunks, the costlier
+// window walks, come first), so a warp that drew cheap cells takes more and
+// the step's barrier waits less for the slowest warp.  Step `t` uses counter
+// t & 1 and clears the other one for step t + 1 (nobody uses it after the
+// previous step's barrier); both start at zero (step_ctr_init).
 // ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void step_ctr_init(SmemFold<R>* sm) {
+    if (threadIdx.x == 0) sm->step_ctr[0] = sm->step_ctr[1] = 0;
+    __syncthreads();
+}
+
 template <typename R, typename GetPL, typename FB, typename FA>
-__device__ __forceinline__ void step_items(SmemFold<R>* sm, int dB, int dA, GetPL getpl, FB fB, FA fA) {
+__device__ __forceinline__ void step_items(SmemFold<R>* sm, int t, int dB, int dA, GetPL getpl, FB fB, FA fA) {
     const int ng = sm->n;
     int NB = 0, NA = 0;
     for (int g = 0; g < ng; ++g) {
@@ -159,7 +172,17 @@ __device__ __forceinline__ void step_items(SmemFold<R>* sm, int dB, int dA, GetP
         if (dA >= 0) NA += max(0, L + 1 - dA);
     }
     const int NB32 = (NB + 31) & ~31;
-    for (int c = threadIdx.x; c < NB32 + NA; c += blockDim.x) {
+    const int total = NB32 + NA;
+    int* ctr = &sm->step_ctr[t & 1];
+    if (threadIdx.x == 0) sm->step_ctr[(t & 1) ^ 1] = 0;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(ctr, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const int c = base + lane;
+        if (c >= total) continue;   // only in the last A chunk (the B block is whole warps)
         if (c < NB32) {
             // B items fill whole warps (NB32 is a multiple of 32): the lanes
             // holding a cell walk it together (see inside_B)
@@ -207,9 +230,10 @@ __device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, con
     const S sr = make_sr<S>(&sm->poly);
     for (int g = 0; g < sm->n; ++g) build_plist(seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).PLs);
     auto getpl = [&](int g) { return in_view<R>(A, sm->ws[g], sm->L[g]).PLs; };
+    step_ctr_init(sm);
     for (int t = 0; t <= sm->Lmax + 1; ++t) {
         step_items(
-            sm, t - 1, t <= sm->Lmax ? t : -1, getpl,
+            sm, t, t - 1, t <= sm->Lmax ? t : -1, getpl,
             [&](int g, int i, unsigned lanes) {   // phase B(t-1): FC of a pairable cell
                 const SeqV Q = seq_v(sm, g);
                 const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
@@ -271,9 +295,10 @@ __device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArg
         exterior_outside_warp(sr, &sm->tabs, seq_v(sm, g), out_tabs(A, sm->ws[g], sm->L[g]));
     __syncthreads();
     auto getpl = [&](int g) { return plist_of(A, sm->ws[g], sm->L[g]); };
+    step_ctr_init(sm);
     for (int t = sm->Lmax; t >= 0; --t) {
         step_items(
-            sm, t - 1, t, getpl,
+            sm, t, t - 1, t, getpl,
             [&](int g, int a, unsigned lanes) {   // phase B(t-1): FCo of a pairable cell
                 const SeqV Q = seq_v(sm, g);
                 outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
