@@ -269,7 +269,7 @@ def our_arm(args):
                 phase += plan.phase_ms()
         plan.status()
         res = {"step_ms": step_ms, "phase_ms": phase / args.steps, "launches": plan.launches * args.steps,
-               "group": plan.group, "arena_bytes": plan.arena_bytes}
+               "group": plan.group, "arena_bytes": plan.arena_bytes, "schedule": plan.schedule}
         plan.close()
         eng.close()
         return res
@@ -279,8 +279,10 @@ def our_arm(args):
     # clock sampler
     plain = run_mode("plain")
     grouped = run_mode("batched", schedule="group")
+    # the batched plan runs untimed per phase: a grouped MEA plan is then one
+    # fused launch per step (per-phase timing would split it into four)
     with ClockSampler(local) as clk:
-        batched = run_mode("batched")
+        batched = run_mode("batched", timing=False)
     clocks = clk.summary()
     structs = d_out.cpu().numpy().reshape(n, L).tobytes().decode("ascii")
     gpu_structs = [structs[b * L:(b + 1) * L] for b in range(n)]
@@ -328,9 +330,12 @@ def our_arm(args):
     from oracle.oracle import OP_COST
     ph = batched["phase_ms"]
     if batched["launches"] == args.steps:
-        # the batched path is one fused kernel: inside + outside + posterior + decode
+        # the batched path is one fused kernel: inside + outside + posterior + decode,
+        # timed by the CUDA events around each step (one launch and a memset)
         phase_cats = {0: tuple(range(8)), 1: (), 2: (), 3: ()}
-        names = {0: "k_fold_warp<MEA>", 1: "-", 2: "-", 3: "-"}
+        fused = {"warp": "k_fold_warp<MEA>", "group": "k_fold_group32<MEA>", "cta": "k_fold_cta<MEA>"}
+        names = {0: fused.get(batched["schedule"], batched["schedule"]), 1: "-", 2: "-", 3: "-"}
+        ph = np.array([statistics.mean(batched["step_ms"]), 0.0, 0.0, 0.0])
     else:
         phase_cats = {0: (0, 1, 2), 1: (3, 4, 5), 2: (6,), 3: (7,)}
         names = {0: "k_inside32", 1: "k_outside32", 2: "k_posterior32", 3: "k_mea32"}

@@ -322,7 +322,7 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (bool wide : {false, true}) {
         const cf::FoldKernels fk = cf::fold_kernels(wide);
-        for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea})
+        for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea, fk.fused_mea, fk.fused_bpp})
             CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     }
     for (int mode = 0; mode < 4; ++mode)
@@ -528,6 +528,10 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                         CF_PHASE(2, (cf::k_plain_posterior32<<<grid, blk, psm, st>>>(Ap)));
                         CF_PHASE(3, (cf::k_plain_mea32<<<grid, blk, psm, st>>>(A)));
                     }
+                    break;
+                }
+                if (X.timer == nullptr) {   // one launch for all phases; per-phase kernels when timing
+                    CF_PHASE(0, ((job == JOB_BPP ? fk.fused_bpp : fk.fused_mea)<<<grid, blkw, smem, st>>>(A)));
                     break;
                 }
                 CF_PHASE(0, (k_in<<<grid, blkw, smem, st>>>(Ai)));
@@ -1008,6 +1012,14 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
     int rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
     p->launches = X.launches;
     return rc;
+}
+
+const char* cf_plan_schedule(const cf_plan* p) {
+    if (!p) return "";
+    if (p->P.plain) return "plain";
+    if (p->P.warp) return "warp";
+    if (p->P.cta) return "cta";
+    return "group";
 }
 
 int cf_plan_set_graph(cf_plan* p, int on) {

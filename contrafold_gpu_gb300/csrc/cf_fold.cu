@@ -438,6 +438,31 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k
 }
 
 // ---------------------------------------------------------------------------
+// Fused grouped fold: one launch runs inside -> outside -> posterior -> MEA
+// decode (MODE 0) or posterior into the caller's matrices (MODE 1) for the
+// CTA's group.  Each CTA goes on to its next phase as soon as its own group
+// is done, instead of every phase waiting for the slowest CTA of the grid.
+// ---------------------------------------------------------------------------
+template <int NT, int MODE>
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_fold_group32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    setup_group(sm, A, A.blob32);
+    inside_group<Lse32>(sm, A);
+    outside_group(sm, A);
+    __syncthreads();
+    if constexpr (MODE == 0) {
+        FoldArgs Ap = A;
+        Ap.post_out = nullptr;
+        Ap.logz = nullptr;
+        posterior_group(sm, Ap);
+        mea_group(sm, A);
+    } else {
+        posterior_group(sm, A);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Persistent fused fold: each CTA takes one sequence at a time from a device
 // work queue and runs inside -> outside -> posterior -> MEA decode (or the
 // inside alone for logZ) before taking the next.  Only one or two sequences
@@ -666,12 +691,19 @@ template __global__ void k_posterior32<kFoldThreadsWide>(FoldArgs);
 template __global__ void k_mea32<kFoldThreads>(FoldArgs);
 template __global__ void k_mea32<kFoldThreadsWide>(FoldArgs);
 
+template __global__ void k_fold_group32<kFoldThreads, 0>(FoldArgs);
+template __global__ void k_fold_group32<kFoldThreads, 1>(FoldArgs);
+template __global__ void k_fold_group32<kFoldThreadsWide, 0>(FoldArgs);
+template __global__ void k_fold_group32<kFoldThreadsWide, 1>(FoldArgs);
+
 FoldKernels fold_kernels(bool wide) {
     if (wide)
         return {k_inside32<kFoldThreadsWide>, k_inside32acc<kFoldThreadsWide>, k_outside32<kFoldThreadsWide>,
-                k_posterior32<kFoldThreadsWide>, k_mea32<kFoldThreadsWide>};
+                k_posterior32<kFoldThreadsWide>, k_mea32<kFoldThreadsWide>,
+                k_fold_group32<kFoldThreadsWide, 0>, k_fold_group32<kFoldThreadsWide, 1>};
     return {k_inside32<kFoldThreads>, k_inside32acc<kFoldThreads>, k_outside32<kFoldThreads>,
-            k_posterior32<kFoldThreads>, k_mea32<kFoldThreads>};
+            k_posterior32<kFoldThreads>, k_mea32<kFoldThreads>,
+            k_fold_group32<kFoldThreads, 0>, k_fold_group32<kFoldThreads, 1>};
 }
 
 size_t fold_smem_bytes(int Lmax, int group, bool fp64) {

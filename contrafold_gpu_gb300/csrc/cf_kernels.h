@@ -41,6 +41,7 @@ struct FoldArgs {
 using FoldKernel = void (*)(FoldArgs);
 struct FoldKernels {
     FoldKernel inside, inside_acc, outside, posterior, mea;
+    FoldKernel fused_mea, fused_bpp;   // k_fold_group32: all phases of MEA / BPP in one launch
 };
 FoldKernels fold_kernels(bool wide);
 __global__ void k_inside64(FoldArgs A);

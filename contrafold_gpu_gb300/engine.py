@@ -27,7 +27,7 @@ SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_
            "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
-           "cf_plan_group", "cf_plan_set_graph", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
+           "cf_plan_group", "cf_plan_set_graph", "cf_plan_schedule", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
            "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats")
 CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE = 0, 1, 3, 4
 
@@ -83,6 +83,8 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_launches.argtypes = [vp]
         L.cf_plan_group.argtypes = [vp]
         L.cf_plan_set_graph.argtypes = [vp, ctypes.c_int]
+        L.cf_plan_schedule.argtypes = [vp]
+        L.cf_plan_schedule.restype = ctypes.c_char_p
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
                      "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
                      "cf_sample_seeded", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
@@ -287,6 +289,11 @@ class Plan:
 
     def set_timing(self, on: bool):
         self.engine._check(self.lib.cf_plan_set_timing(self._h, 1 if on else 0))
+
+    @property
+    def schedule(self) -> str:
+        """'plain', 'warp', 'cta' or 'group'."""
+        return self.lib.cf_plan_schedule(self._h).decode()
 
     def set_graph(self, on: bool):
         """Replay the plan's launches as one CUDA graph while run arguments repeat."""

@@ -200,6 +200,10 @@ int cf_plan_launches(const cf_plan* plan);
  * launches that graph -- one launch call for all the plan's kernels and
  * memsets.  New arguments re-capture.  Ignored while phase timing is on. */
 int cf_plan_set_graph(cf_plan* plan, int on);
+/* The plan's schedule: "plain", "warp", "cta" or "group" (static string).  A
+ * grouped MEA / BPP plan runs all phases in one launch (k_fold_group32) unless
+ * phase timing is on, which runs the per-phase kernels. */
+const char* cf_plan_schedule(const cf_plan* plan);
 int cf_plan_group(const cf_plan* plan);
 
 /* ---- serving loop: continuous batching of single-sequence requests ----

@@ -62,3 +62,33 @@ def test_plan_matches_host_calls_with_and_without_graph(engine, schedule):
                         assert np.array_equal(o, np.asarray(ref)), (job, graph)
     finally:
         engine.set_schedule("auto")
+
+
+def test_phase_timing_runs_the_per_phase_kernels(engine):
+    """With phase timing on, a grouped MEA plan runs four per-phase kernels
+    instead of the fused one; structures are identical and the phases timed."""
+    torch = pytest.importorskip("torch")
+    from contrafold_gpu_gb300.engine import CF_JOB_MEA, Batch, Plan
+    engine.set_schedule("group")
+    try:
+        seqs, masks = _batch(11, 90, 30, 160)
+        d_seqs, d_mask, offs = _device(torch, seqs, masks)
+        tot = int(offs[-1])
+        outs = {}
+        for timing in (False, True):
+            plan = Plan(engine, CF_JOB_MEA, offs)
+            assert plan.schedule == "group"
+            plan.set_timing(timing)
+            out = torch.zeros(tot, dtype=torch.uint8, device="cuda")
+            plan.run(d_seqs.data_ptr(), d_mask.data_ptr(), out.data_ptr(), 6.0, 0)
+            plan.status()
+            torch.cuda.synchronize()
+            outs[timing] = out.cpu().numpy().tobytes()
+            assert plan.launches == (4 if timing else 1)
+            if timing:
+                assert np.all(plan.phase_ms() > 0)
+            plan.close()
+        assert outs[False] == outs[True]
+        assert outs[False].decode() == "".join(engine.mea(Batch(seqs, masks), 6.0))
+    finally:
+        engine.set_schedule("auto")
