@@ -6,6 +6,8 @@
     gpu-contrafold GGGGAAAACCCC --sample 10      # 10 Boltzmann samples
     gpu-contrafold GGGGAAAACCCC --logz           # partition function (logZ)
     gpu-contrafold seqs.jsonl -o out.jsonl       # batch (JSONL in/out)
+    gpu-contrafold seqs.fa --parens out.parens   # structures also as a CONTRAfold parens file
+    gpu-contrafold seqs.fa --posteriors 1e-5 out.post   # sparse posterior file (CONTRAfold format)
 
 Same arguments, input sniffing, mask validation, mode precedence and output
 format as the reference (cli.py:88-230).  The difference is where the work
@@ -23,6 +25,11 @@ JSONL input (one object per line):
 Output: a single literal sequence prints structures to stdout (one per line);
 file input (or any -o) writes JSONL ({"id","structure"}, or {"id","samples":[...]}
 for --sample N, or {"id","logZ"} for --logz), input order preserved.
+
+--parens FILE and --posteriors CUTOFF FILE take the CONTRAfold binary's
+`predict` options of the same names (the reference reads those files in
+gpu_contrafold/reference.py:61-132): the structures, and the base-pair
+posteriors >= CUTOFF, written in that binary's file formats (`formats.py`).
 """
 from __future__ import annotations
 
@@ -148,6 +155,21 @@ def fold(records, P, mode="mea", sample_n=0, with_logz=False, gamma=6.0, chunk=4
     return logz, samples, structures
 
 
+def posteriors(records, P, chunk=4096):
+    """Base-pair probability matrices of the records (GPU, length-sorted
+    chunks), in input order."""
+    from . import gpu
+    seqs = [r[1] for r in records]
+    masks = [build_mask(r[1], r[2], where=f"id={r[0]!r}: ") for r in records]
+    order = sorted(range(len(records)), key=lambda k: len(seqs[k]))
+    out = [None] * len(records)
+    for c0 in range(0, len(records), chunk):
+        idx = order[c0:c0 + chunk]
+        for k, m in zip(idx, gpu.bpp_batch([seqs[k] for k in idx], P, forced_list=[masks[k] for k in idx])):
+            out[k] = m
+    return out
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     if argv and argv[0] == "fold":          # back-compat: optional 'fold' subcommand
@@ -168,7 +190,17 @@ def main(argv=None):
     parser.add_argument("--threads", type=int, default=128,
                         help="accepted for compatibility; the engine picks its own launch shape")
     parser.add_argument("--seed", type=int, default=0, help="RNG seed for sampling")
+    parser.add_argument("--parens", default=None, metavar="FILE",
+                        help="also write the structures as a CONTRAfold parens file (>id, sequence, structure)")
+    parser.add_argument("--posteriors", nargs=2, default=None, metavar=("CUTOFF", "FILE"),
+                        help="also write base-pair posteriors >= CUTOFF in CONTRAfold's sparse format")
     args = parser.parse_args(argv)
+    cutoff = None
+    if args.posteriors is not None:
+        try:
+            cutoff = float(args.posteriors[0])
+        except ValueError:
+            raise SystemExit(f"--posteriors: cutoff {args.posteriors[0]!r} is not a number")
 
     records, from_file = load_records(args.input)
     if not records:
@@ -182,11 +214,19 @@ def main(argv=None):
         mode = "mfe"
     else:
         mode = "mea"
+    if args.parens and mode not in ("mea", "mfe"):
+        raise SystemExit("--parens writes structures: not with --sample or --logz")
 
     from .params import load
     P = load()
     logz, samples, structures = fold(records, P, mode=mode, sample_n=args.sample, with_logz=args.logz,
                                      gamma=args.gamma, chunk=args.chunk, seed=args.seed)
+    from . import formats
+    if args.parens:
+        formats.write_parens_file(args.parens, [(r[0], r[1], st) for r, st in zip(records, structures)])
+    if args.posteriors is not None:
+        mats = posteriors(records, P, chunk=args.chunk)
+        formats.write_posteriors_file(args.posteriors[1], [(r[0], r[1], m) for r, m in zip(records, mats)], cutoff)
 
     if not from_file and not args.output:
         if mode in ("mfe", "mea"):

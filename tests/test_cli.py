@@ -79,3 +79,47 @@ def test_cli_end_to_end(tmp_path, P, oracle, golden):
     assert [g["structure"] for g in got] == [c["mea"]["6.0"] for c in recs]
     r = _run([str(src), "-o", str(out), "--viterbi"], repo)
     assert [json.loads(l)["structure"] for l in open(out)] == [c["mfe"] for c in recs]
+
+
+@pytest.mark.gpu
+def test_cli_contrafold_files(tmp_path, golden):
+    """--parens / --posteriors: the binary's file formats, read back as the
+    reference reads them, equal the golden MEA structures and posteriors."""
+    import os
+
+    from conftest import golden_post
+    from contrafold_gpu_gb300 import formats
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    recs = [c for c in golden["cases"] if 8 <= len(c["seq"]) <= 80][:10]
+    src = tmp_path / "in.jsonl"
+    with open(src, "w") as fh:
+        for k, c in enumerate(recs):
+            obj = {"id": f"s{k}", "seq": c["seq"]}
+            if c["mask"]:
+                obj["constrain"] = c["mask"]
+            fh.write(json.dumps(obj) + "\n")
+    par, post, out = tmp_path / "o.parens", tmp_path / "o.post", tmp_path / "o.jsonl"
+    r = _run([str(src), "-o", str(out), "--parens", str(par), "--posteriors", "1e-4", str(post)], repo)
+    assert r.returncode == 0, r.stderr
+    lines = par.read_text().splitlines()
+    assert len(lines) == 3 * len(recs)
+    for k, c in enumerate(recs):
+        assert lines[3 * k:3 * k + 3] == [f">s{k}", c["seq"], c["mea"]["6.0"]]
+    blocks, cur = [], None
+    for line in post.read_text().splitlines():
+        if line.startswith(">"):
+            cur = []
+            blocks.append(cur)
+        else:
+            cur.append(line)
+    assert len(blocks) == len(recs)
+    for k, c in enumerate(recs):
+        L = len(c["seq"])
+        one = tmp_path / f"one{k}.post"
+        one.write_text("\n".join(blocks[k]) + "\n")
+        got = formats.read_posteriors(str(one), L)
+        want = np.triu(golden_post(c)[1:L + 1, 1:L + 1].astype(np.float64), 1)
+        keep = want >= 1e-4
+        assert np.allclose(got[keep], want[keep], rtol=5e-6, atol=0) and np.all(got[~keep] == 0)
+    r = _run(["GGGGAAAACCCC", "--logz", "--parens", str(par)], repo)
+    assert r.returncode != 0 and "--parens" in r.stderr
