@@ -107,7 +107,7 @@ struct cf_engine {
     DevBuf<double> counts, unpaired;
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
     int mode = 1;        // 0 plain, 1 batched
-    int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent
+    int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent, 3 grouped, 4 cluster
     int ctas_per_sm = 0; // CTA-persistent occupancy cap (0 = auto)
     int group = 0;       // sequences per CTA of the grouped kernels (0 = auto)
     size_t smem_optin = 0;
@@ -126,6 +126,10 @@ namespace {
 // 172k vs 186k, n=4096 238k vs 191k.
 int auto_warp_max_len() { return 256; }
 int auto_warp_min_batch(int Lmax) { return Lmax <= 80 ? 4096 : 2048; }
+// Small batches of long sequences fold on a thread-block cluster each
+// (GB300, MEA: one 600-nt fold 172 -> 144 ms, 1,000 nt 450 -> 297 ms,
+// 32 x 600 nt 184 -> 158 ms; 64 x 300 nt stays grouped: 69 vs 125 ms).
+int auto_cluster_min_len() { return 512; }
 // CTAs per SM of the persistent CTA kernel by length.
 int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
 
@@ -142,6 +146,7 @@ struct Plan {
     bool plain = false;           // reference launch shape (mode 0): cf_plain.cu kernels for BPP/MEA
     bool cta = false;             // persistent CTA-per-sequence fused kernel (batched path)
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
+    bool cluster = false;         // a thread-block cluster per group (latency of long sequences)
     int wgrid = 0;                // its grid
     int64_t slot_words = 0;       // its arena slot per warp
     std::vector<SeqDesc> descs;   // grouped order
@@ -215,9 +220,17 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // Mixed lengths stay one plan, longest first: splitting a 40-400 nt batch
     // at 256 nt into a warp-kernel part and a grouped part on two streams was
     // slower for every job (MEA 8.5k vs 10.7k folds/s).
+    if (sched == 0 && batched && Lmin >= auto_cluster_min_len() &&
+        (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE)) {
+        int sms = 0;
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        if ((int64_t)n * cf::kClusterCtas <= (int64_t)cf::kClusterMinBlocks * sms) sched = 4;
+    }
     if (sched == 0)
         sched = (job != JOB_SAMPLE && !uniform && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch(P.Lmax))
                     ? 1 : 3;
+    P.cluster = batched && sched == 4 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
+    if (P.cluster) P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group) : 1;
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
@@ -329,6 +342,9 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
         CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (int mode = 0; mode < 3; ++mode)
         CF_CUDA(cudaFuncSetAttribute(cf::cta_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    const cf::ClusterKernels ck = cf::cluster_kernels();
+    for (cf::FoldKernel k : {ck.mea, ck.bpp, ck.inside_acc})
+        CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     eng->smem_optin = bytes;
     return CF_OK;
 }
@@ -504,9 +520,13 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         const cf::FoldKernels fk = cf::fold_kernels(wide);
         const cf::FoldKernel k_in = fk.inside, k_inacc = fk.inside_acc, k_out = fk.outside, k_post = fk.posterior,
                              k_dec = fk.mea;
+        // cluster schedule: every group on kClusterCtas CTAs of one cluster
+        const cf::ClusterKernels ck = cf::cluster_kernels();
+        const dim3 cgrid(grid * cf::kClusterCtas);
         switch (job) {
             case JOB_LOGZ:
-                CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
+                if (P.cluster) CF_PHASE(0, (ck.inside_acc<<<cgrid, blk, smem, st>>>(A)));
+                else CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
                 break;
             case JOB_LOGZ64:
                 CF_PHASE(0, (cf::k_inside64<<<grid, blk, smem, st>>>(A)));
@@ -530,6 +550,10 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                     }
                     break;
                 }
+                if (P.cluster) {   // fused only: the phases are timed as one
+                    CF_PHASE(0, ((job == JOB_BPP ? ck.bpp : ck.mea)<<<cgrid, blk, smem, st>>>(A)));
+                    break;
+                }
                 if (X.timer == nullptr) {   // one launch for all phases; per-phase kernels when timing
                     CF_PHASE(0, ((job == JOB_BPP ? fk.fused_bpp : fk.fused_mea)<<<grid, blkw, smem, st>>>(A)));
                     break;
@@ -551,7 +575,8 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                 CF_PHASE(0, (cf::k_viterbi64<<<grid, blk, smem, st>>>(A)));
                 break;
             case JOB_SAMPLE: {
-                CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
+                if (P.cluster) CF_PHASE(0, (ck.inside_acc<<<cgrid, blk, smem, st>>>(A)));
+                else CF_PHASE(0, (k_inacc<<<grid, blkw, smem, st>>>(A)));
                 if (!sj || sj->n_samples <= 0) break;
                 cf::SampleArgs S;
                 S.descs = A.descs;
@@ -749,7 +774,7 @@ int cf_engine_set_mode(cf_engine* e, int mode) {
 
 int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
-    if (kind < 0 || kind > 3 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
+    if (kind < 0 || kind > 4 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
     e->sched = kind;
     e->ctas_per_sm = ctas_per_sm;
     return CF_OK;
@@ -1019,6 +1044,7 @@ const char* cf_plan_schedule(const cf_plan* p) {
     if (p->P.plain) return "plain";
     if (p->P.warp) return "warp";
     if (p->P.cta) return "cta";
+    if (p->P.cluster) return "cluster";
     return "group";
 }
 

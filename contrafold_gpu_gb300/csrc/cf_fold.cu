@@ -63,10 +63,53 @@ __device__ __forceinline__ void build_group_seqs(SmemFold<R>* sm, const FoldArgs
     __syncthreads();
 }
 
-// Load tables, group descriptors, sequence codes and partner bit sets.
+// ---------------------------------------------------------------------------
+// Teams: the threads that fold one group together.  CtaTeam is one CTA (the
+// batched kernels); ClusterTeam is the C CTAs of a thread-block cluster, on C
+// SMs, folding the same group (the latency kernels).  Work of a diagonal step
+// is split over tid() / nthreads(); sync() separates steps (a cluster barrier
+// with release / acquire semantics for ClusterTeam, so table cells written in
+// global memory by one CTA are read by the others after it).  Every sync() is
+// reached by all threads of the team: the loops around them run the same trip
+// counts in every CTA (each CTA loads the same group descriptors), and
+// rank-0-only work sits between two syncs, not around one.
+// ---------------------------------------------------------------------------
+struct CtaTeam {
+    static constexpr int kRowPF = 1;   // window-walk loads in flight per lane (lockstep_row)
+    static constexpr int kChainPF = cf::kChainPF;   // bifurcation-chain register pipeline depth
+    __device__ __forceinline__ int rank() const { return 0; }
+    __device__ __forceinline__ int size() const { return 1; }
+    __device__ __forceinline__ int tid() const { return threadIdx.x; }
+    __device__ __forceinline__ int nthreads() const { return blockDim.x; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+
+struct ClusterTeam {
+    static constexpr int kRowPF = CF_CLUSTER_ROW_PF;
+    static constexpr int kChainPF = CF_CLUSTER_CHAIN_PF;
+    int r, c;   // rank of this CTA in the cluster, cluster size
+    __device__ __forceinline__ int rank() const { return r; }
+    __device__ __forceinline__ int size() const { return c; }
+    __device__ __forceinline__ int tid() const { return r * blockDim.x + threadIdx.x; }
+    __device__ __forceinline__ int nthreads() const { return c * blockDim.x; }
+    __device__ __forceinline__ void sync() const {
+        asm volatile("barrier.cluster.arrive.release;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
+    }
+};
+
+__device__ __forceinline__ int cluster_ctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+    return (int)r;
+}
+
+// Load tables, group descriptors, sequence codes and partner bit sets of
+// group `gi` (default: this CTA's index).
 template <typename R>
-__device__ __forceinline__ void setup_group(SmemFold<R>* sm, const FoldArgs& A, const R* __restrict__ gblob) {
-    const int g0 = blockIdx.x * A.group;
+__device__ __forceinline__ void setup_group(SmemFold<R>* sm, const FoldArgs& A, const R* __restrict__ gblob,
+                                            int gi = -1) {
+    const int g0 = (gi < 0 ? (int)blockIdx.x : gi) * A.group;
     const int ng = min(A.group, A.n - g0);
     if (threadIdx.x == 0) {
         int lmax = 0;
@@ -151,7 +194,9 @@ __device__ __forceinline__ PairList plist_of(const FoldArgs& A, int64_t ws_off, 
 // window walks, come first), so a warp that drew cheap cells takes more and
 // the step's barrier waits less for the slowest warp.  Step `t` uses counter
 // t & 1 and clears the other one for step t + 1 (nobody uses it after the
-// previous step's barrier); both start at zero (step_ctr_init).
+// previous step's barrier); both start at zero (step_ctr_init).  In a cluster
+// team the step's chunks are dealt round-robin to the CTAs (chunk k to rank
+// k mod size) and each CTA's warps claim its chunks from its own counter.
 // ---------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void step_ctr_init(SmemFold<R>* sm) {
@@ -159,8 +204,8 @@ __device__ __forceinline__ void step_ctr_init(SmemFold<R>* sm) {
     __syncthreads();
 }
 
-template <typename R, typename GetPL, typename FB, typename FA>
-__device__ __forceinline__ void step_items(SmemFold<R>* sm, int t, int dB, int dA, GetPL getpl, FB fB, FA fA) {
+template <typename R, class Team, typename GetPL, typename FB, typename FA>
+__device__ __forceinline__ void step_items(SmemFold<R>* sm, const Team& tm, int t, int dB, int dA, GetPL getpl, FB fB, FA fA) {
     const int ng = sm->n;
     int NB = 0, NA = 0;
     for (int g = 0; g < ng; ++g) {
@@ -177,9 +222,11 @@ __device__ __forceinline__ void step_items(SmemFold<R>* sm, int t, int dB, int d
     if (threadIdx.x == 0) sm->step_ctr[(t & 1) ^ 1] = 0;
     const int lane = threadIdx.x & 31;
     for (;;) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(ctr, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        // the CTA's q-th chunk is chunk q * size + rank of the team's step
+        int q = 0;
+        if (lane == 0) q = atomicAdd(ctr, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        const int base = (q * tm.size() + tm.rank()) * 32;
         if (base >= total) break;
         const int c = base + lane;
         if (c >= total) continue;   // only in the last A chunk (the B block is whole warps)
@@ -207,7 +254,7 @@ __device__ __forceinline__ void step_items(SmemFold<R>* sm, int t, int dB, int d
             }
         }
     }
-    __syncthreads();
+    tm.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -224,33 +271,36 @@ __device__ __forceinline__ Lse64 make_sr<Lse64>(const PolyTables*) { return Lse6
 template <>
 __device__ __forceinline__ Max64 make_sr<Max64>(const PolyTables*) { return Max64{}; }
 
-template <class S>
-__device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, const FoldArgs& A) {
+template <class S, class Team = CtaTeam>
+__device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, const FoldArgs& A, const Team tm = Team{}) {
     using R = typename S::Real;
     const S sr = make_sr<S>(&sm->poly);
-    for (int g = 0; g < sm->n; ++g) build_plist(seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).PLs);
+    if (tm.rank() == 0)
+        for (int g = 0; g < sm->n; ++g) build_plist(seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).PLs);
+    if (tm.size() > 1) tm.sync();   // the pair lists, for every CTA of the team
     auto getpl = [&](int g) { return in_view<R>(A, sm->ws[g], sm->L[g]).PLs; };
     step_ctr_init(sm);
     for (int t = 0; t <= sm->Lmax + 1; ++t) {
         step_items(
-            sm, t, t - 1, t <= sm->Lmax ? t : -1, getpl,
+            sm, tm, t, t - 1, t <= sm->Lmax ? t : -1, getpl,
             [&](int g, int i, unsigned lanes) {   // phase B(t-1): FC of a pairable cell
                 const SeqV Q = seq_v(sm, g);
                 const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
                 const R fm2 = V.FB[((t - 1) & 1) * V.fbs + i];
-                inside_B<S>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2, lanes);
+                inside_B<S, Team::kRowPF>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2, lanes);
             },
             [&](int g, int i) {   // phase A(t): FM2, FM1, FM
                 const SeqV Q = seq_v(sm, g);
                 const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
-                V.FB[(t & 1) * V.fbs + i] = inside_A<S>(sr, &sm->tabs, Q, V.T, i, i + t);
+                V.FB[(t & 1) * V.fbs + i] = inside_A<S, Team::kChainPF>(sr, &sm->tabs, Q, V.T, i, i + t);
             });
     }
     // exterior recurrence: one warp per sequence
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int g = warp; g < sm->n; g += nwarps)
-        exterior_warp<S>(sr, &sm->tabs, seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).T);
-    __syncthreads();
+    if (tm.rank() == 0)
+        for (int g = warp; g < sm->n; g += nwarps)
+            exterior_warp<S>(sr, &sm->tabs, seq_v(sm, g), in_view<R>(A, sm->ws[g], sm->L[g]).T);
+    tm.sync();
 }
 
 template <int NT>
@@ -288,42 +338,45 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_inside64(FoldA
 // ---------------------------------------------------------------------------
 // Outside + posterior + MEA (FP32)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArgs& A) {
+template <class Team = CtaTeam>
+__device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArgs& A, const Team tm = Team{}) {
     const Lse32 sr{&sm->poly};
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int g = warp; g < sm->n; g += nwarps)
-        exterior_outside_warp(sr, &sm->tabs, seq_v(sm, g), out_tabs(A, sm->ws[g], sm->L[g]));
-    __syncthreads();
+    if (tm.rank() == 0)
+        for (int g = warp; g < sm->n; g += nwarps)
+            exterior_outside_warp(sr, &sm->tabs, seq_v(sm, g), out_tabs(A, sm->ws[g], sm->L[g]));
+    tm.sync();
     auto getpl = [&](int g) { return plist_of(A, sm->ws[g], sm->L[g]); };
     step_ctr_init(sm);
     for (int t = sm->Lmax; t >= 0; --t) {
         step_items(
-            sm, t, t - 1, t, getpl,
+            sm, tm, t, t - 1, t, getpl,
             [&](int g, int a, unsigned lanes) {   // phase B(t-1): FCo of a pairable cell
                 const SeqV Q = seq_v(sm, g);
-                outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
+                outside_B<Team::kRowPF>(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
             },
             [&](int g, int a) {   // phase A(t): FMo, FM1o, FM2o
                 const SeqV Q = seq_v(sm, g);
-                outside_A_merged(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t);
+                outside_A_merged<Team::kChainPF>(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t);
             });
     }
 }
 
 // Posterior of every pairable pair; POST goes to the FMo slot (triangular,
 // zero elsewhere) and, for cf_bpp, densely into the caller's L x L matrix.
-__device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldArgs& A) {
+template <class Team = CtaTeam>
+__device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldArgs& A, const Team tm = Team{}) {
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         float* POST = out_tabs(A, sm->ws[g], L).FMo;
         const int64_t tot = tri_size(L);
-        for (int64_t c = threadIdx.x; c < tot; c += blockDim.x) POST[c] = 0.0f;
+        for (int64_t c = tm.tid(); c < tot; c += tm.nthreads()) POST[c] = 0.0f;
         if (A.post_out) {
             float* dense = A.post_out + A.post_offs[sm->idx[g]];
-            for (int64_t c = threadIdx.x; c < (int64_t)L * L; c += blockDim.x) dense[c] = 0.0f;
+            for (int64_t c = tm.tid(); c < (int64_t)L * L; c += tm.nthreads()) dense[c] = 0.0f;
         }
     }
-    __syncthreads();
+    tm.sync();
     for (int g = 0; g < sm->n; ++g) {
         const SeqV Q = seq_v(sm, g);
         const int L = Q.L, m = L + 1;
@@ -333,22 +386,22 @@ __device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldA
         float* POST = T.FMo;
         float* dense = A.post_out ? A.post_out + A.post_offs[sm->idx[g]] : nullptr;
         // pairable FC cells (i, i+d) <-> pairs (a, b) = (i, i+d+1), in list
-        // order, whole warps at a time (thread k takes entries k, k + blockDim, ...)
+        // order, whole warps at a time (team thread k takes entries k, k + nthreads, ...)
         const int total = PLs.poff[L + 1];
         const int lane = threadIdx.x & 31;
-        for (int c0 = threadIdx.x - lane; c0 < total; c0 += blockDim.x) {
+        for (int c0 = tm.tid() - lane; c0 < total; c0 += tm.nthreads()) {
             const int c = c0 + lane;
             const unsigned lanes = __ballot_sync(0xffffffffu, c < total);
             if (c >= total) continue;
             const int d = plist_diag(PLs, L, c);
             const int a = PLs.pl[c], b = a + d + 1;
-            const float v = posterior_pair(&sm->tabs, &sm->poly, Q, T, Z, a, b, lanes);
+            const float v = posterior_pair<Team::kRowPF>(&sm->tabs, &sm->poly, Q, T, Z, a, b, lanes);
             POST[tri_off(d + 1, m) + a] = v;
             if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
         }
     }
-    __syncthreads();
-    if (A.logz != nullptr)
+    tm.sync();
+    if (A.logz != nullptr && tm.rank() == 0)
         for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
             const OutTabs T = out_tabs(A, sm->ws[g], sm->L[g]);
             A.logz[sm->idx[g]] = T.F5[sm->L[g]];
@@ -373,13 +426,13 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k
 
 // Walk diagonals d = d_begin .. d_end (step +1) over all sequences of the
 // group; call f(g, i, i + d) for every cell.  One barrier per diagonal.
-template <typename R, typename F>
-__device__ __forceinline__ void wavefront(SmemFold<R>* sm, int d_begin, int d_end, int step, F f) {
+template <typename R, class Team, typename F>
+__device__ __forceinline__ void wavefront(SmemFold<R>* sm, const Team& tm, int d_begin, int d_end, int step, F f) {
     const int ng = sm->n;
     for (int d = d_begin; step > 0 ? d <= d_end : d >= d_end; d += step) {
         int total = 0;
         for (int g = 0; g < ng; ++g) total += max(0, sm->L[g] + 1 - d);
-        for (int c = threadIdx.x; c < total; c += blockDim.x) {
+        for (int c = tm.tid(); c < total; c += tm.nthreads()) {
             int g = 0, r = c;
             while (true) {
                 const int cnt = max(0, sm->L[g] + 1 - d);
@@ -389,42 +442,44 @@ __device__ __forceinline__ void wavefront(SmemFold<R>* sm, int d_begin, int d_en
             }
             f(g, r, r + d);
         }
-        __syncthreads();
+        tm.sync();
     }
 }
 
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
 // with the reference's strict-'>' candidate order, BFS traceback.
-__device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A) {
+template <class Team = CtaTeam>
+__device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A, const Team tm = Team{}) {
     const float two_g = __fmul_rn(2.0f, A.gamma);
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         const Arena32 ar = arena32(L);
         float* base = A.ws + sm->ws[g];
-        for (int i = 1 + threadIdx.x; i <= L; i += blockDim.x) base[ar.up + i] = mea_unpaired(base + ar.FMo, L, two_g, i);
+        for (int i = 1 + tm.tid(); i <= L; i += tm.nthreads()) base[ar.up + i] = mea_unpaired(base + ar.FMo, L, two_g, i);
     }
-    __syncthreads();
-    wavefront(sm, 0, sm->Lmax, +1, [&](int g, int i, int j) {
+    tm.sync();
+    wavefront(sm, tm, 0, sm->Lmax, +1, [&](int g, int i, int j) {
         const SeqV Q = seq_v(sm, g);
         const Arena32 ar = arena32(Q.L);
         float* base = A.ws + sm->ws[g];
-        mea_cell(Q, base + ar.FMo, base + ar.up, base + ar.FM2o, reinterpret_cast<int*>(base + ar.FM), Q.L, i, j);
+        mea_cell<Team::kChainPF>(Q, base + ar.FMo, base + ar.up, base + ar.FM2o, reinterpret_cast<int*>(base + ar.FM), Q.L, i, j);
     });
     for (int g = 0; g < sm->n; ++g) {
         const int L = sm->L[g];
         char* out = A.structs + sm->soff[g];
-        for (int t = threadIdx.x; t < L; t += blockDim.x) out[t] = '.';
+        for (int t = tm.tid(); t < L; t += tm.nthreads()) out[t] = '.';
     }
-    __syncthreads();
-    for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
-        const int L = sm->L[g];
-        const Arena32 ar = arena32(L);
-        float* base = A.ws + sm->ws[g];
-        int* qi = reinterpret_cast<int*>(base + ar.queue);
-        mea_traceback(reinterpret_cast<const int*>(base + ar.FM), L, qi, qi + 2 * L + 4, A.structs + sm->soff[g],
-                      A.status);
-    }
-    __syncthreads();
+    tm.sync();
+    if (tm.rank() == 0)
+        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
+            const int L = sm->L[g];
+            const Arena32 ar = arena32(L);
+            float* base = A.ws + sm->ws[g];
+            int* qi = reinterpret_cast<int*>(base + ar.queue);
+            mea_traceback(reinterpret_cast<const int*>(base + ar.FM), L, qi, qi + 2 * L + 4, A.structs + sm->soff[g],
+                          A.status);
+        }
+    tm.sync();
 }
 
 // MEA decode (cpu.py:823-895): unpaired weights, gamma-weighted max-plus DP
@@ -459,6 +514,42 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k
         mea_group(sm, A);
     } else {
         posterior_group(sm, A);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Cluster fold (latency of long sequences): the kClusterCtas CTAs of a
+// thread-block cluster, on as many SMs, fold one group together -- each
+// diagonal step's cells are dealt over all of them, with a cluster barrier
+// between steps; the serial exterior recurrences and the traceback run on
+// rank 0.  MODE 0: MEA, 1: BPP (as k_fold_group32); 2: the inside with the
+// accurate log-sum-exp alone (logZ, and the tables the sampler draws from).
+// No CTA touches another's shared memory, so CTAs may leave independently.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kFoldThreads, kClusterMinBlocks)
+    k_fold_cluster32(FoldArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
+    const ClusterTeam tm{cluster_ctarank(), kClusterCtas};
+    setup_group(sm, A, A.blob32, (int)blockIdx.x / kClusterCtas);
+    if constexpr (MODE == 2) {
+        inside_group<LseAcc32>(sm, A, tm);
+        if (A.logz != nullptr && tm.rank() == 0)
+            for (int g = threadIdx.x; g < sm->n; g += blockDim.x)
+                A.logz[sm->idx[g]] = in_view<float>(A, sm->ws[g], sm->L[g]).T.F5[sm->L[g]];
+    } else {
+        inside_group<Lse32>(sm, A, tm);
+        outside_group(sm, A, tm);
+        if constexpr (MODE == 0) {
+            FoldArgs Ap = A;
+            Ap.post_out = nullptr;
+            Ap.logz = nullptr;
+            posterior_group(sm, Ap, tm);
+            mea_group(sm, A, tm);
+        } else {
+            posterior_group(sm, A, tm);
+        }
     }
 }
 
@@ -704,6 +795,10 @@ FoldKernels fold_kernels(bool wide) {
     return {k_inside32<kFoldThreads>, k_inside32acc<kFoldThreads>, k_outside32<kFoldThreads>,
             k_posterior32<kFoldThreads>, k_mea32<kFoldThreads>,
             k_fold_group32<kFoldThreads, 0>, k_fold_group32<kFoldThreads, 1>};
+}
+
+ClusterKernels cluster_kernels() {
+    return {k_fold_cluster32<0>, k_fold_cluster32<1>, k_fold_cluster32<2>};
 }
 
 size_t fold_smem_bytes(int Lmax, int group, bool fp64) {

@@ -125,7 +125,8 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 //     goes to the slot read at term k - 1, whose value the fold of term k - 1
 //     has already consumed.  The module defines CF_CHAIN_THREADS (its block
 //     size); float chains only.
-//   CF_CHAIN_PF = PF > 0: a rolling register pipeline of 2*PF terms.
+//   CF_CHAIN_PF = PF > 0: a rolling register pipeline of 2*PF terms (the
+//     default of the PFD template parameter; latency kernels pass a deeper one).
 //   both 0: load, then fold.
 // ---------------------------------------------------------------------------
 #ifndef CF_CHAIN_PF
@@ -158,7 +159,7 @@ __device__ __forceinline__ void cp_async_wait() {
 __shared__ float cf_chain_ring[CF_CHAIN_ASYNC + 1][2][CF_CHAIN_THREADS];
 #endif
 
-template <typename R, class Ld, class Step>
+template <typename R, int PFD = kChainPF, class Ld, class Step>
 __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
 #if CF_CHAIN_ASYNC > 0
     if constexpr (sizeof(R) == 4) {
@@ -207,14 +208,14 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
         return;
     }
 #endif
-    if constexpr (kChainPF == 0) {
+    if constexpr (PFD == 0) {
         for (int k = 0; k < n; ++k) {
             const R *px, *py;
             ld(px, py);
             step(k, *px, *py);
         }
     } else {
-        R xa[kChainPF], ya[kChainPF], xb[kChainPF], yb[kChainPF];
+        R xa[PFD], ya[PFD], xb[PFD], yb[PFD];
         auto load = [&](R& x, R& y) {
             const R *px, *py;
             ld(px, py);
@@ -222,17 +223,17 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
             y = *py;
         };
 #pragma unroll
-        for (int u = 0; u < kChainPF; ++u)
+        for (int u = 0; u < PFD; ++u)
             if (u < n) load(xa[u], ya[u]);
-        for (int k0 = 0; k0 < n; k0 += kChainPF) {
+        for (int k0 = 0; k0 < n; k0 += PFD) {
 #pragma unroll
-            for (int u = 0; u < kChainPF; ++u)
-                if (k0 + kChainPF + u < n) load(xb[u], yb[u]);
+            for (int u = 0; u < PFD; ++u)
+                if (k0 + PFD + u < n) load(xb[u], yb[u]);
 #pragma unroll
-            for (int u = 0; u < kChainPF; ++u)
+            for (int u = 0; u < PFD; ++u)
                 if (k0 + u < n) step(k0 + u, xa[u], ya[u]);
 #pragma unroll
-            for (int u = 0; u < kChainPF; ++u) {
+            for (int u = 0; u < PFD; ++u) {
                 xa[u] = xb[u];
                 ya[u] = yb[u];
             }
@@ -243,9 +244,12 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
 // One row of a lockstep window walk (see inside_B): every lane of the group
 // runs `slots` iterations (the largest candidate count among them) and takes
 // the set bits of its own mask, highest first (HI) or lowest first; the
-// table value of the next candidate, `ld(bit)`, is loaded before the current
-// one is used, `use(bit, v)`.
-template <bool HI, typename R, class Ld, class Use>
+// table values of the next PF candidates, `ld(bit)`, are loaded before the
+// current one is used, `use(bit, v)`.  PF = 1 (one load ahead) suits the
+// throughput kernels, whose many warps cover the load latency; the latency
+// kernels, where one cell's walk is the critical path of a step, keep more
+// loads in flight.  The candidates are used in the same order for every PF.
+template <bool HI, int PF = 1, typename R, class Ld, class Use>
 __device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use use) {
     auto take = [&](int& bit) -> bool {
         if (msk == 0u) return false;
@@ -258,19 +262,44 @@ __device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use
         }
         return true;
     };
-    int bit = 0;
-    R v = R(0);
-    bool h = take(bit);
-    if (h) v = ld(bit);
-    for (int k = 0; k < slots; ++k) {
-        int bn = 0;
-        R vn = R(0);
-        const bool hn = take(bn);
-        if (hn) vn = ld(bn);
-        if (h) use(bit, v);
-        h = hn;
-        bit = bn;
-        v = vn;
+    if constexpr (PF == 1) {
+        int bit = 0;
+        R v = R(0);
+        bool h = take(bit);
+        if (h) v = ld(bit);
+        for (int k = 0; k < slots; ++k) {
+            int bn = 0;
+            R vn = R(0);
+            const bool hn = take(bn);
+            if (hn) vn = ld(bn);
+            if (h) use(bit, v);
+            h = hn;
+            bit = bn;
+            v = vn;
+        }
+    } else {
+        // ring of PF candidates: slot u holds candidate k0 + u; once used it
+        // takes candidate k0 + u + PF (the next one not yet taken)
+        int bits[PF];
+        R vals[PF];
+        bool has[PF];
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+            bits[u] = 0;
+            vals[u] = R(0);
+            has[u] = take(bits[u]);
+            if (has[u]) vals[u] = ld(bits[u]);
+        }
+        for (int k0 = 0; k0 < slots; k0 += PF) {
+#pragma unroll
+            for (int u = 0; u < PF; ++u) {
+                if (k0 + u < slots) {
+                    if (has[u]) use(bits[u], vals[u]);
+                    has[u] = take(bits[u]);
+                    if (has[u]) vals[u] = ld(bits[u]);
+                }
+            }
+        }
     }
 }
 
@@ -286,7 +315,7 @@ __device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use
 // Phase A of inside cell (i, j), 0 <= i <= j <= L.  Returns FM2[i][j] (the
 // semiring zero where the cell needs none).  Writes FM1, FM, and FC = zero
 // for cells that cannot close a pair (pairable cells get FC in phase B).
-template <class S, class QV>
+template <class S, int CPF = kChainPF, class QV>
 __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
                                                      const QV& Q, const InTabs<typename S::Real>& T, int i, int j) {
     using R = typename S::Real;
@@ -310,7 +339,7 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
         int o1 = tri_off(1, m) + i;          // FM1[i][i+1]
         int o2 = tri_off(d - 1, m) + i + 1;  // FM[i+1][j]
         int s1 = 1, s2 = d - 1;
-        prefetched_chain<R>(
+        prefetched_chain<R, CPF>(
             d - 1,
             [&](const R*& x, const R*& y) {
                 x = T.FM1 + o1;
@@ -370,7 +399,7 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
 // lane with fewer candidates idles in the remaining slots, so the warp never
 // splits into per-lane paths; each lane still folds exactly its own
 // candidates in the reference's order.
-template <class S, class QV>
+template <class S, int PF = 1, class QV>
 __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
                                          const QV& Q, const InTabs<typename S::Real>& T, int i, int j,
                                          typename S::Real fm2, unsigned lanes) {
@@ -393,7 +422,7 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         const R sn1 = l1 == 0 ? P.b01(sj) : (l1 == 1 ? P.i11(si1, sj) : R(0));
         uint32_t msk = l1 < nrows ? Q.window(p + 1, qlo, j - qlo + 1) : 0u;
         const int slots = __reduce_max_sync(lanes, __popc(msk));
-        lockstep_row<true, R>(
+        lockstep_row<true, PF, R>(
             msk, slots, [&](int bit) -> R { return T.FC[tri_off(qlo + bit - 2 - p, m) + p + 1]; },
             [&](int bit, R v) {
                 if (!(v > HALF)) return;

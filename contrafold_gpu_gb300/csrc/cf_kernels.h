@@ -44,6 +44,23 @@ struct FoldKernels {
     FoldKernel fused_mea, fused_bpp;   // k_fold_group32: all phases of MEA / BPP in one launch
 };
 FoldKernels fold_kernels(bool wide);
+// k_fold_cluster32: one group folded by the kClusterCtas CTAs of a cluster
+// (grid = groups x kClusterCtas, kFoldThreads per CTA)
+constexpr int kClusterCtas = 8;
+#ifndef CF_CLUSTER_ROW_PF
+#define CF_CLUSTER_ROW_PF 1   // window-walk loads in flight per lane in the cluster kernels
+#endif
+#ifndef CF_CLUSTER_CHAIN_PF
+#define CF_CLUSTER_CHAIN_PF 8   // bifurcation-chain pipeline depth in the cluster kernels
+#endif
+#ifndef CF_CLUSTER_MIN_BLOCKS
+#define CF_CLUSTER_MIN_BLOCKS 2   // resident CTAs per SM the cluster kernels' registers target
+#endif
+constexpr int kClusterMinBlocks = CF_CLUSTER_MIN_BLOCKS;
+struct ClusterKernels {
+    FoldKernel mea, bpp, inside_acc;
+};
+ClusterKernels cluster_kernels();
 __global__ void k_inside64(FoldArgs A);
 __global__ void k_viterbi64(FoldArgs A);
 

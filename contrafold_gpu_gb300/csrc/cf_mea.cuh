@@ -23,7 +23,7 @@ __device__ __forceinline__ float mea_unpaired(const float* __restrict__ POST, in
 }
 
 // One DP cell (i, j) of the decode.  QV provides pairable(a, b).
-template <class QV>
+template <int CPF = kChainPF, class QV>
 __device__ __forceinline__ void mea_cell(const QV& Q, const float* __restrict__ POST, const float* __restrict__ up,
                                          float* __restrict__ score, int* __restrict__ tb, int L, int i, int j) {
     const int m = L + 1;
@@ -48,7 +48,7 @@ __device__ __forceinline__ void mea_cell(const QV& Q, const float* __restrict__ 
         int o1 = tri_off(1, m) + i;               // score[i][i+1]
         int o2 = tri_off(j - i - 1, m) + i + 1;   // score[i+1][j]
         int s1 = 1, s2 = j - i - 1;
-        prefetched_chain<float>(
+        prefetched_chain<float, CPF>(
             j - i - 1,
             [&](const float*& x, const float*& y) {
                 x = score + o1;

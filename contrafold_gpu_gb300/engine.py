@@ -174,8 +174,10 @@ class Engine:
         self.mode = mode
 
     def set_schedule(self, kind: str = "auto", ctas_per_sm: int = 0):
-        """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap) or 'group'."""
-        self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3}[kind],
+        """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap), 'group' or
+        'cluster' (each sequence folded by a thread-block cluster: latency of long sequences)."""
+        self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3,
+                                                              "cluster": 4}[kind],
                                                     int(ctas_per_sm)))
 
     def set_group(self, group: int = 0):

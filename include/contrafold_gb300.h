@@ -93,11 +93,15 @@ int cf_engine_set_budget(cf_engine* eng, size_t bytes);
 int cf_engine_set_mode(cf_engine* eng, int mode);
 /* Batched-path schedule (the tuner's knob): kind 0 = automatic by length,
  * 1 = persistent warp-per-sequence kernel, 2 = persistent CTA-per-sequence
- * fused kernel, 3 = length-grouped per-phase kernels (kind 0 takes the warp
- * kernel for batches of >= 2048 sequences of <= 256 nt -- 4096 up to 80 nt --
- * except for sampling, else kind 3); ctas_per_sm caps the
- * persistent CTA kernel's residency (0 = automatic).  Results are identical
- * for every choice. */
+ * fused kernel, 3 = length-grouped per-phase kernels, 4 = cluster: each
+ * sequence (or group, cf_engine_set_group) folded by the 8 CTAs of a
+ * thread-block cluster on 8 SMs -- the latency of long sequences, for logZ,
+ * BPP, MEA and sampling (kind 0 takes the cluster kernels when every
+ * sequence has >= 512 nt and the batch fills at most two clusters' worth of
+ * CTAs per SM, the warp kernel for batches of >= 2048 sequences of <= 256 nt
+ * -- 4096 up to 80 nt -- except for sampling, else kind 3); ctas_per_sm caps
+ * the persistent CTA kernel's residency (0 = automatic).  Results are
+ * identical for every choice. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
 /* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32, or
  * 0 = automatic (by the median length, capped to keep two CTAs per SM).  The
@@ -200,7 +204,8 @@ int cf_plan_launches(const cf_plan* plan);
  * launches that graph -- one launch call for all the plan's kernels and
  * memsets.  New arguments re-capture.  Ignored while phase timing is on. */
 int cf_plan_set_graph(cf_plan* plan, int on);
-/* The plan's schedule: "plain", "warp", "cta" or "group" (static string).  A
+/* The plan's schedule: "plain", "warp", "cta", "group" or "cluster" (static
+ * string).  A
  * grouped MEA / BPP plan runs all phases in one launch (k_fold_group32) unless
  * phase timing is on, which runs the per-phase kernels. */
 const char* cf_plan_schedule(const cf_plan* plan);

@@ -104,7 +104,7 @@ def test_cli_contrafold_files(tmp_path, golden):
     lines = par.read_text().splitlines()
     assert len(lines) == 3 * len(recs)
     for k, c in enumerate(recs):
-        assert lines[3 * k:3 * k + 3] == [f">s{k}", c["seq"], c["mea"]["6.0"]]
+        assert lines[3 * k:3 * k + 3] == [f">s{k}", c["seq"].upper(), c["mea"]["6.0"]]
     blocks, cur = [], None
     for line in post.read_text().splitlines():
         if line.startswith(">"):

@@ -18,7 +18,7 @@ from conftest import golden_post, mask_of
 pytestmark = pytest.mark.gpu
 
 
-PATHS = ["plain", "warp", "cta", "group"]
+PATHS = ["plain", "warp", "cta", "group", "cluster"]
 
 
 def set_path(engine, path):
@@ -147,7 +147,7 @@ def test_plain_equals_batched(engine):
         res[path] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B), z, np.concatenate([m.ravel() for m in mats]))
     set_path(engine, "cta")
     engine.set_schedule("auto")
-    for path in ("warp", "cta", "group"):
+    for path in ("warp", "cta", "group", "cluster"):
         assert np.array_equal(res["plain"][0], res[path][0])
         assert res["plain"][1] == res[path][1]
         assert res["plain"][2] == res[path][2]
@@ -220,3 +220,25 @@ def test_long_sequence_vs_oracle(engine, P, oracle):
     assert abs(engine.logz64(B)[0] - z64) <= 1e-9 * abs(z64)
     # float32 logZ: the 5e-4 of the 200-nt contract, scaled with the length (600 / 200)
     assert abs(engine.logz(B)[0] - z64) <= 5e-4 * 3
+
+
+def test_long_sequence_cluster_vs_oracle(engine, P, oracle):
+    """The cluster schedule (one 8-CTA cluster per sequence) on 600 and 1,000 nt:
+    MEA identical to the oracle, BPP bitwise equal to the grouped kernels."""
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(62, 2, 600, 1000, 0.1)
+    B = Batch(seqs, masks)
+    try:
+        engine.set_schedule("group")
+        mats_g, z_g = engine.bpp(B)
+        lz_g = engine.logz(B)
+        engine.set_schedule("cluster")
+        got = engine.mea(B, 6.0)
+        mats_c, z_c = engine.bpp(B)
+        assert np.array_equal(engine.logz(B), lz_g)
+    finally:
+        engine.set_schedule("auto")
+    assert got[0] == oracle.mea(seqs[0], P, 6.0, masks[0])
+    assert z_c.tobytes() == z_g.tobytes()
+    for a, b in zip(mats_c, mats_g):
+        assert a.tobytes() == b.tobytes()

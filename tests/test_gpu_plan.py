@@ -22,7 +22,7 @@ def _device(torch, seqs, masks):
     return torch.from_numpy(buf).to(dev), torch.from_numpy(mk).to(dev), offs
 
 
-@pytest.mark.parametrize("schedule", ["auto", "warp", "group"])
+@pytest.mark.parametrize("schedule", ["auto", "warp", "group", "cluster"])
 def test_plan_matches_host_calls_with_and_without_graph(engine, schedule):
     torch = pytest.importorskip("torch")
     from contrafold_gpu_gb300.engine import CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE, Batch, Plan
@@ -92,3 +92,17 @@ def test_phase_timing_runs_the_per_phase_kernels(engine):
         assert outs[False].decode() == "".join(engine.mea(Batch(seqs, masks), 6.0))
     finally:
         engine.set_schedule("auto")
+
+
+def test_auto_schedule_takes_cluster_for_small_long_batches(engine):
+    """Automatic schedule: a few sequences of >= 512 nt fold on a cluster each;
+    a larger batch of 300-nt sequences stays grouped."""
+    from contrafold_gpu_gb300.engine import CF_JOB_LOGZ, CF_JOB_MEA, Plan
+    engine.set_schedule("auto")
+    for job in (CF_JOB_MEA, CF_JOB_LOGZ):
+        plan = Plan(engine, job, np.array([0, 600, 1300], np.int64))
+        assert plan.schedule == "cluster"
+        plan.close()
+    plan = Plan(engine, CF_JOB_MEA, np.arange(65, dtype=np.int64) * 300)
+    assert plan.schedule == "group"
+    plan.close()
