@@ -10,6 +10,12 @@ auto_warp_max_len / auto_ctas_per_sm) is set from these measurements.
 
     python -m contrafold_gpu_gb300.autotune [--lengths 50,100,200,300,400] [--json out.json]
     python -m contrafold_gpu_gb300.autotune --lengths 100,200 --batch-sizes 256,1024,4096
+    python -m contrafold_gpu_gb300.autotune --latency --lengths 150,400,600,1000 --batch-sizes 1,16,32
+
+--latency times small batches of long sequences (ms per batch) on the grouped
+and the cluster schedules -- the engine's auto_cluster_min_len -- and, with
+--phase-timing, the grouped schedule's per-phase kernels; --mask-frac sets the
+forced-unpaired fraction (1.0: no pairable cell, the bifurcation chains alone).
 """
 from __future__ import annotations
 
@@ -20,12 +26,39 @@ import time
 import numpy as np
 
 
-def _batch_bytes(n, L, seed):
+def _batch_bytes(n, L, seed, mask_frac=0.1):
     rng = np.random.default_rng(seed)
     idx = rng.integers(0, 4, size=(n, L), dtype=np.int8)
     seq = np.frombuffer(b"ACGU", np.uint8)[idx].reshape(-1).copy()
-    mask = (rng.random((n, L)) < 0.1).astype(np.uint8).reshape(-1)
+    mask = (rng.random((n, L)) < mask_frac).astype(np.uint8).reshape(-1)
     return seq, mask
+
+
+def time_latency(P, L, n, kind, job="mea", mask_frac=0.1, phases=False, reps=3):
+    """Best wall time (ms) of one batch of n sequences of L nt on schedule
+    `kind`, and the per-phase device times when `phases` (per-phase kernels)."""
+    import torch
+    from .engine import CF_JOB_LOGZ, CF_JOB_MEA, Engine, Plan
+    seq, mask = _batch_bytes(n, L, 7, mask_frac)
+    dev = torch.device("cuda", 0)
+    d_seq = torch.from_numpy(seq).to(dev)
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_out = torch.empty(n * L if job == "mea" else 4 * n, dtype=torch.uint8, device=dev)
+    eng = Engine(P)
+    eng.set_schedule(kind)
+    plan = Plan(eng, CF_JOB_MEA if job == "mea" else CF_JOB_LOGZ, np.arange(n + 1, dtype=np.int64) * L)
+    plan.set_timing(phases)
+    stream = torch.cuda.Stream(dev)
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        plan.run(d_seq.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+        plan.status()
+        best = min(best, (time.perf_counter() - t0) * 1e3)
+    ph = [round(float(x), 2) for x in plan.phase_ms()] if phases else None
+    plan.close()
+    eng.close()
+    return best, ph
 
 
 def time_schedule(P, L, n, kind, ctas, reps=3, job="mea", group=0):
@@ -71,9 +104,26 @@ def main():
     ap.add_argument("--groups", default=None,
                     help="comma list: time the grouped schedule with each number of sequences per CTA at every "
                          "length (batch sized as for the schedule table) -- the engine's group_for_length table")
+    ap.add_argument("--latency", action="store_true",
+                    help="ms per small batch on the grouped and cluster schedules (lengths x --batch-sizes)")
+    ap.add_argument("--mask-frac", type=float, default=0.1, help="--latency: forced-unpaired fraction")
+    ap.add_argument("--phase-timing", action="store_true", help="--latency: grouped per-phase kernel times")
     args = ap.parse_args()
     from . import load
     P = load()
+    if args.latency:
+        table = {}
+        for L in [int(x) for x in args.lengths.split(",")]:
+            for n in [int(x) for x in (args.batch_sizes or "1").split(",")]:
+                g_ms, ph = time_latency(P, L, n, "group", args.job, args.mask_frac, args.phase_timing)
+                c_ms, _ = time_latency(P, L, n, "cluster", args.job, args.mask_frac)
+                table[f"{L}x{n}"] = {"group_ms": g_ms, "cluster_ms": c_ms, "group_phase_ms": ph}
+                print(f"L={L:4d} n={n:4d} group {g_ms:8.2f} ms  cluster {c_ms:8.2f} ms"
+                      + (f"  group phases {ph}" if ph else ""), flush=True)
+        if args.json:
+            with open(args.json, "w") as fh:
+                json.dump(table, fh, indent=1)
+        return table
     if args.groups:
         table = {}
         for L in [int(x) for x in args.lengths.split(",")]:
