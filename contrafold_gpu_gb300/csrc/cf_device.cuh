@@ -100,11 +100,12 @@ __host__ __device__ __forceinline__ Arena64 arena64(int L) {
 // segments.  The evaluation order ((c0*d + c1)*d + c2)*d + c3 is the
 // reference's.
 //
-// Segment lookup: with u = 4d (exact), bin = floor(u) in 0..47 holds at most
-// one boundary (boundaries are >= 0.86 apart, bins 0.25 wide), so
-// seg = (boundaries below the bin) + (d >= the boundary inside the bin), read
-// from a 48-entry table -- the same count as comparing d with all seven.
-// Fast_Exp uses the same scheme on u = -4x over its five boundaries.
+// Segment lookup: bin = floor(d) in 0..11 holds at most one boundary (the
+// boundaries 0.66, 1.63, 2.49, 3.38, 4.43, 5.79, 7.82 fall in distinct unit
+// intervals), so seg = (boundaries below the bin) + (d >= the boundary inside
+// the bin), read from a 12-entry table -- the same count as comparing d with
+// all seven.  Fast_Exp uses the same scheme on u = -x over its five
+// boundaries (0.67, 1.48, 2.49, 3.84, 5.86: distinct unit intervals too).
 // ---------------------------------------------------------------------------
 #define LSE_T0 ((float)0.6615367791)
 #define LSE_T1 ((float)1.6320158198)
@@ -122,8 +123,8 @@ __host__ __device__ __forceinline__ Arena64 arena64(int L) {
 #define FEXP_T4 ((float)-1.4805375919)
 #define FEXP_T5 ((float)-0.6725053211)
 
-constexpr int kLseBins = 48;    // 0.25-wide bins of d over [0, 12)
-constexpr int kFexpBins = 40;   // 0.25-wide bins of -x over [0, 10)
+constexpr int kLseBins = 12;    // unit bins of d over [0, 12)
+constexpr int kFexpBins = 10;   // unit bins of -x over [0, 10)
 
 struct PolyTables {
     float4 lse[8];
@@ -158,7 +159,7 @@ __device__ __forceinline__ void load_poly_tables(PolyTables* t) {
         } else if (k < 16 + kLseBins) {
             if (k >= 16) {
                 const int b = k - 16;
-                const float lo = __fmul_rn((float)b, 0.25f), hi = __fmul_rn((float)(b + 1), 0.25f);
+                const float lo = (float)b, hi = (float)(b + 1);
                 const float T[7] = {LSE_T0, LSE_T1, LSE_T2, LSE_T3, LSE_T4, LSE_T5, LSE_T6};
                 int base = 0;
                 float inner = 3.402823466e38f;
@@ -170,7 +171,7 @@ __device__ __forceinline__ void load_poly_tables(PolyTables* t) {
             }
         } else if (k < 16 + kLseBins + kFexpBins) {
             const int b = k - 16 - kLseBins;
-            const float lo = __fmul_rn((float)b, 0.25f), hi = __fmul_rn((float)(b + 1), 0.25f);
+            const float lo = (float)b, hi = (float)(b + 1);
             const float U[5] = {-FEXP_T1, -FEXP_T2, -FEXP_T3, -FEXP_T4, -FEXP_T5};
             int base = 0;   // boundaries U_k >= hi: u <= U_k for every u of the bin
             float inner = -3.402823466e38f;
@@ -199,11 +200,15 @@ __device__ __forceinline__ float lse32(const PolyTables* __restrict__ pt, float 
     const float hi = fmaxf(a, b);
     const float lo = fminf(a, b);
     const float d = __fsub_rn(hi, lo);
-    const float2 e = pt->lse_bin[min(__float2int_rz(__fmul_rn(d, 4.0f)), kLseBins - 1)];
+    const float2 e = pt->lse_bin[min(__float2int_rz(d), kLseBins - 1)];
     const int seg = __float_as_int(e.y) + (d >= e.x);
     const float r = cubic(pt->lse[seg], d);
     const float res = __fadd_rn(lo, r);
-    return (lo < CF_HALF32 || d >= LSE_TMAX) ? hi : res;
+    // The reference also returns hi when lo is below the zero threshold; for
+    // finite inputs that case is covered: lo < -5e29 < hi makes d at least
+    // one float spacing there (~4e22) >= LSE_TMAX, and lo == hi gives
+    // res = lo + cubic(0) == lo (0.69 is far below half a spacing of lo).
+    return d >= LSE_TMAX ? hi : res;
 }
 
 // exp(x), CONTRAfold Fast_Exp (RealT = float).  For x >= 0 the reference
@@ -214,7 +219,7 @@ __device__ __forceinline__ float fexp32(const PolyTables* __restrict__ pt, float
         return (float)exp((double)x);
     }
     const float u = -x;   // x < 0: x >= T_k  <=>  u <= -T_k
-    const float2 e = pt->fexp_bin[min(__float2int_rz(__fmul_rn(u, 4.0f)), kFexpBins - 1)];
+    const float2 e = pt->fexp_bin[min(__float2int_rz(u), kFexpBins - 1)];
     const int seg = __float_as_int(e.y) + (u <= e.x);
     const float r = cubic(pt->fexp[seg], x);
     return x < FEXP_T0 ? 0.0f : r;

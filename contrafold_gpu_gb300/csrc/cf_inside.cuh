@@ -225,7 +225,21 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
 #pragma unroll
         for (int u = 0; u < PFD; ++u)
             if (u < n) load(xa[u], ya[u]);
-        for (int k0 = 0; k0 < n; k0 += PFD) {
+        int k0 = 0;
+        // whole blocks: the next block's loads and this block's steps are all
+        // in range, so no per-term checks
+        for (; k0 + 2 * PFD <= n; k0 += PFD) {
+#pragma unroll
+            for (int u = 0; u < PFD; ++u) load(xb[u], yb[u]);
+#pragma unroll
+            for (int u = 0; u < PFD; ++u) step(k0 + u, xa[u], ya[u]);
+#pragma unroll
+            for (int u = 0; u < PFD; ++u) {
+                xa[u] = xb[u];
+                ya[u] = yb[u];
+            }
+        }
+        for (; k0 < n; k0 += PFD) {
 #pragma unroll
             for (int u = 0; u < PFD; ++u)
                 if (k0 + PFD + u < n) load(xb[u], yb[u]);
