@@ -439,7 +439,10 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         lockstep_row<true, PF, R>(
             msk, slots, [&](int bit) -> R { return T.FC[tri_off(qlo + bit - 2 - p, m) + p + 1]; },
             [&](int bit, R v) {
-                if (!(v > HALF)) return;
+                // no zero-threshold test on v: a visited candidate is a
+                // pairable cell, whose FC always holds its hairpin term, and
+                // acc (likewise) is finite, so a sub-threshold v would leave
+                // acc unchanged in any case
                 const int q = qlo + bit;
                 const int l2 = j - q, a = p + 1;
                 R e;
