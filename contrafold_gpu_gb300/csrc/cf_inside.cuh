@@ -26,7 +26,7 @@ struct Lse32 {
 };
 
 // float32 log-sum-exp with accurate log1pf/expf.  Used where the result is
-// judged against the FP64 engine (logZ within 5e-4) rather than bitwise
+// compared with the FP64 engine (logZ within 5e-4) rather than bitwise
 // against the reference's Fast_LogPlusEquals arithmetic.
 struct LseAcc32 {
     using Real = float;

@@ -8,7 +8,7 @@
 // the fold itself needs little; and a latency-bound serving loop, where
 // cudaFree waits for the whole device and stalls every other stream.  This
 // entry point instead works inside one fixed array in device global memory,
-// reserved by the driver when this module is loaded.
+// reserved by the CUDA driver when this module is loaded.
 //
 // What it runs.  The MEA mode of the persistent warp-per-sequence kernel
 // (cf_warp.cu), the same code cf_mea's batched path launches for short
@@ -36,7 +36,7 @@
 //
 // Set-up.  The first call on each device (with that device current) resolves
 // the scratch's device address with cudaGetSymbolAddress, which also makes the
-// driver load this module if it is loaded lazily.  Make that first call before
+// CUDA driver load this module if it is loaded lazily.  Make that first call before
 // any stream capture begins.
 #include <cuda_runtime.h>
 

@@ -278,7 +278,7 @@ int cf_server_stats(cf_server* server, double* stats, int32_t n_stats);
  * Numba on every call.  Same arguments, results and argument errors as cf_mea,
  * but the call allocates no device memory: inputs, descriptors, outputs and the
  * fold arenas live in one static device array of CF_SCRATCH_BYTES, reserved by
- * the driver when the library's module is loaded.  For callers that cannot let
+ * the CUDA driver when the library's module is loaded.  For callers that cannot let
  * a library allocate while they run (a framework allocator has reserved the
  * device; cudaFree would stall a serving loop's other streams).
  * - Batches whose inputs, outputs and 8 fold slots for the longest sequence do

@@ -66,7 +66,7 @@ def test_golden_covers_edge_cases(golden):
 
 
 def test_oracle_batch_driver(P, golden, oracle):
-    """The threaded batch driver (CPU baseline) returns what the single calls return."""
+    """The threaded batch runner (CPU baseline) returns what the single calls return."""
     recs = golden["cases"][20:60]
     seqs = [r["seq"] for r in recs]
     masks = [mask_of(r) for r in recs]
