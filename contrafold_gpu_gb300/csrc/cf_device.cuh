@@ -40,7 +40,10 @@ __host__ __device__ __forceinline__ int64_t tri_size(int L) {
     const int64_t m = L + 1;
     return m * (m + 1) / 2;
 }
-__host__ __device__ __forceinline__ int tri_off(int d, int m) { return d * m - (d * (d - 1)) / 2; }
+// d * (d - 1) is never negative (d and d - 1 share a sign or one is 0) and
+// below 2^31 for d <= 32,768, so the halving is a shift (no signed-division
+// rounding fix-up).
+__host__ __device__ __forceinline__ int tri_off(int d, int m) { return d * m - ((d * (d - 1)) >> 1); }
 
 // Round a word count up to 32 words (128 bytes).
 __host__ __device__ __forceinline__ int64_t pad32(int64_t w) { return (w + 31) & ~int64_t(31); }
