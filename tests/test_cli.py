@@ -123,3 +123,15 @@ def test_cli_contrafold_files(tmp_path, golden):
         assert np.allclose(got[keep], want[keep], rtol=5e-6, atol=0) and np.all(got[~keep] == 0)
     r = _run(["GGGGAAAACCCC", "--logz", "--parens", str(par)], repo)
     assert r.returncode != 0 and "--parens" in r.stderr
+
+
+def test_contrafold_file_options_validated_before_folding(tmp_path):
+    """--parens needs a structure mode and --posteriors a numeric cutoff; both are
+    rejected before any sequence is folded (no GPU needed)."""
+    with pytest.raises(SystemExit, match="--parens"):
+        cli.main(["GGGGAAAACCCC", "--logz", "--parens", str(tmp_path / "a.parens")])
+    with pytest.raises(SystemExit, match="--parens"):
+        cli.main(["GGGGAAAACCCC", "--sample", "3", "--parens", str(tmp_path / "a.parens")])
+    with pytest.raises(SystemExit, match="not a number"):
+        cli.main(["GGGGAAAACCCC", "--posteriors", "abc", str(tmp_path / "a.post")])
+    assert not (tmp_path / "a.parens").exists() and not (tmp_path / "a.post").exists()
