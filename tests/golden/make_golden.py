@@ -19,13 +19,21 @@ Run once in a container that has the reference checkout:
     python tests/golden/make_golden.py [--ref /root/reference] [--jobs 8]
 The output, tests/golden/golden.json (+ params_blob64.npy), is committed; the
 tests read only those files.
+
+    python tests/golden/make_golden.py --exhaustive
+writes tests/golden/exhaustive.json.gz instead: every ACGU sequence of 1-5 nt
+without a mask and every (sequence, mask) pair of 1-4 nt, each with FP64 logZ,
+the Viterbi and MEA (gamma 6) structures and the first 16 hex digits of the
+SHA-256 of its float32 posterior matrix.
 """
 from __future__ import annotations
 
 import argparse
 import base64
+import gzip
 import hashlib
 import importlib.util
+import itertools
 import json
 import multiprocessing as mp
 import os
@@ -113,6 +121,27 @@ def _run_case(args):
     return rec
 
 
+def _run_small(args):
+    """Compact record of one exhaustive case: seq, mask bits, logZ, Viterbi,
+    MEA (gamma 6), posterior digest."""
+    seq, mask = args
+    rec = _run_case((seq, mask, [6.0], False))
+    return [seq, rec["mask"] or "", rec["logz64"], rec["mfe"], rec["mea"]["6.0"], rec["post_sha256"][:16]]
+
+
+def exhaustive_cases():
+    cases = []
+    for L in range(1, 6):
+        for t in itertools.product("ACGU", repeat=L):
+            cases.append(("".join(t), None))
+    for L in range(1, 5):
+        for t in itertools.product("ACGU", repeat=L):
+            for m in itertools.product((0, 1), repeat=L):
+                if any(m):
+                    cases.append(("".join(t), list(m)))
+    return cases
+
+
 def rand_seq(rng, L, alphabet="ACGU"):
     return "".join(rng.choice(np.array(list(alphabet)), size=L))
 
@@ -167,8 +196,23 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
-    ap.add_argument("--out", default=os.path.join(HERE, "golden.json"))
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--exhaustive", action="store_true", help="all short sequences (and masks): exhaustive.json.gz")
     args = ap.parse_args()
+    if args.exhaustive:
+        cases = exhaustive_cases()
+        t0 = time.time()
+        with mp.get_context("spawn").Pool(args.jobs, initializer=_init, initargs=(args.ref,)) as pool:
+            rows = pool.map(_run_small, cases, chunksize=64)
+        out = args.out or os.path.join(HERE, "exhaustive.json.gz")
+        doc = {"generator": "tests/golden/make_golden.py --exhaustive",
+               "reference": "gpu_contrafold/cpu.py (pure Python under an identity numba.njit)",
+               "fields": ["seq", "mask", "logz64", "mfe", "mea_gamma6", "post_sha256_16"], "cases": rows}
+        with gzip.open(out, "wt") as fh:
+            json.dump(doc, fh, separators=(",", ":"))
+        print(f"wrote {len(rows)} cases to {out} in {time.time() - t0:.0f}s")
+        return
+    args.out = args.out or os.path.join(HERE, "golden.json")
 
     R = load_reference(args.ref)
     P = R.load()
