@@ -6,7 +6,9 @@
 // path).  The CTA walks the DP diagonals of all its sequences in lock step;
 // on each diagonal the threads take the cells of every sequence of the group
 // (flattened), so short diagonals of several sequences fill the warps that one
-// sequence alone would leave idle.  One __syncthreads separates diagonals.
+// sequence alone would leave idle.  One barrier separates diagonals.  The
+// cluster kernels give a group to the CTAs of a thread-block cluster instead
+// of one CTA (a "team", below), with a cluster barrier between diagonals.
 #include "cf_kernels.h"
 #include "cf_mea.cuh"
 #include "cf_outside.cuh"
