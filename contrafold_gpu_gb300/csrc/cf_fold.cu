@@ -77,7 +77,6 @@ __device__ __forceinline__ void build_group_seqs(SmemFold<R>* sm, const FoldArgs
 // rank-0-only work sits between two syncs, not around one.
 // ---------------------------------------------------------------------------
 struct CtaTeam {
-    static constexpr int kRowPF = 1;   // window-walk loads in flight per lane (lockstep_row)
     static constexpr int kChainPF = cf::kChainPF;   // bifurcation-chain register pipeline depth
     __device__ __forceinline__ int rank() const { return 0; }
     __device__ __forceinline__ int size() const { return 1; }
@@ -87,7 +86,6 @@ struct CtaTeam {
 };
 
 struct ClusterTeam {
-    static constexpr int kRowPF = CF_CLUSTER_ROW_PF;
     static constexpr int kChainPF = CF_CLUSTER_CHAIN_PF;
     int r, c;   // rank of this CTA in the cluster, cluster size
     __device__ __forceinline__ int rank() const { return r; }
@@ -289,7 +287,7 @@ __device__ __forceinline__ void inside_group(SmemFold<typename S::Real>* sm, con
                 const SeqV Q = seq_v(sm, g);
                 const InView<R> V = in_view<R>(A, sm->ws[g], Q.L);
                 const R fm2 = V.FB[((t - 1) & 1) * V.fbs + i];
-                inside_B<S, Team::kRowPF>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2, lanes);
+                inside_B<S>(sr, &sm->tabs, Q, V.T, i, i + t - 1, fm2, lanes);
             },
             [&](int g, int i) {   // phase A(t): FM2, FM1, FM
                 const SeqV Q = seq_v(sm, g);
@@ -355,7 +353,7 @@ __device__ __forceinline__ void outside_group(SmemFold<float>* sm, const FoldArg
             sm, tm, t, t - 1, t, getpl,
             [&](int g, int a, unsigned lanes) {   // phase B(t-1): FCo of a pairable cell
                 const SeqV Q = seq_v(sm, g);
-                outside_B<Team::kRowPF>(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
+                outside_B(sr, &sm->tabs, Q, out_tabs(A, sm->ws[g], Q.L), a, a + t - 1, lanes);
             },
             [&](int g, int a) {   // phase A(t): FMo, FM1o, FM2o
                 const SeqV Q = seq_v(sm, g);
@@ -397,7 +395,7 @@ __device__ __forceinline__ void posterior_group(SmemFold<float>* sm, const FoldA
             if (c >= total) continue;
             const int d = plist_diag(PLs, L, c);
             const int a = PLs.pl[c], b = a + d + 1;
-            const float v = posterior_pair<Team::kRowPF>(&sm->tabs, &sm->poly, Q, T, Z, a, b, lanes);
+            const float v = posterior_pair(&sm->tabs, &sm->poly, Q, T, Z, a, b, lanes);
             POST[tri_off(d + 1, m) + a] = v;
             if (dense != nullptr) dense[(int64_t)(a - 1) * L + (b - 1)] = v;
         }

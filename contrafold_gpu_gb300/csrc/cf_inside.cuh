@@ -258,12 +258,10 @@ __device__ __forceinline__ void prefetched_chain(int n, Ld ld, Step step) {
 // One row of a lockstep window walk (see inside_B): every lane of the group
 // runs `slots` iterations (the largest candidate count among them) and takes
 // the set bits of its own mask, highest first (HI) or lowest first; the
-// table values of the next PF candidates, `ld(bit)`, are loaded before the
-// current one is used, `use(bit, v)`.  PF = 1 (one load ahead) suits the
-// throughput kernels, whose many warps cover the load latency; the latency
-// kernels, where one cell's walk is the critical path of a step, keep more
-// loads in flight.  The candidates are used in the same order for every PF.
-template <bool HI, int PF = 1, typename R, class Ld, class Use>
+// table value of the next candidate, `ld(bit)`, is loaded before the current
+// one is used, `use(bit, v)`.  (Two to eight loads ahead measured slower, in
+// the batched and in the cluster kernels alike.)
+template <bool HI, typename R, class Ld, class Use>
 __device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use use) {
     auto take = [&](int& bit) -> bool {
         if (msk == 0u) return false;
@@ -276,44 +274,19 @@ __device__ __forceinline__ void lockstep_row(uint32_t msk, int slots, Ld ld, Use
         }
         return true;
     };
-    if constexpr (PF == 1) {
-        int bit = 0;
-        R v = R(0);
-        bool h = take(bit);
-        if (h) v = ld(bit);
-        for (int k = 0; k < slots; ++k) {
-            int bn = 0;
-            R vn = R(0);
-            const bool hn = take(bn);
-            if (hn) vn = ld(bn);
-            if (h) use(bit, v);
-            h = hn;
-            bit = bn;
-            v = vn;
-        }
-    } else {
-        // ring of PF candidates: slot u holds candidate k0 + u; once used it
-        // takes candidate k0 + u + PF (the next one not yet taken)
-        int bits[PF];
-        R vals[PF];
-        bool has[PF];
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-            bits[u] = 0;
-            vals[u] = R(0);
-            has[u] = take(bits[u]);
-            if (has[u]) vals[u] = ld(bits[u]);
-        }
-        for (int k0 = 0; k0 < slots; k0 += PF) {
-#pragma unroll
-            for (int u = 0; u < PF; ++u) {
-                if (k0 + u < slots) {
-                    if (has[u]) use(bits[u], vals[u]);
-                    has[u] = take(bits[u]);
-                    if (has[u]) vals[u] = ld(bits[u]);
-                }
-            }
-        }
+    int bit = 0;
+    R v = R(0);
+    bool h = take(bit);
+    if (h) v = ld(bit);
+    for (int k = 0; k < slots; ++k) {
+        int bn = 0;
+        R vn = R(0);
+        const bool hn = take(bn);
+        if (hn) vn = ld(bn);
+        if (h) use(bit, v);
+        h = hn;
+        bit = bn;
+        v = vn;
     }
 }
 
@@ -413,7 +386,7 @@ __device__ __forceinline__ typename S::Real inside_A(const S& sr, const SmemTabs
 // lane with fewer candidates idles in the remaining slots, so the warp never
 // splits into per-lane paths; each lane still folds exactly its own
 // candidates in the reference's order.
-template <class S, int PF = 1, class QV>
+template <class S, class QV>
 __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S::Real>* __restrict__ tb,
                                          const QV& Q, const InTabs<typename S::Real>& T, int i, int j,
                                          typename S::Real fm2, unsigned lanes) {
@@ -436,7 +409,7 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         const R sn1 = l1 == 0 ? P.b01(sj) : (l1 == 1 ? P.i11(si1, sj) : R(0));
         uint32_t msk = l1 < nrows ? Q.window(p + 1, qlo, j - qlo + 1) : 0u;
         const int slots = __reduce_max_sync(lanes, __popc(msk));
-        lockstep_row<true, PF, R>(
+        lockstep_row<true, R>(
             msk, slots, [&](int bit) -> R { return T.FC[tri_off(qlo + bit - 2 - p, m) + p + 1]; },
             [&](int bit, R v) {
                 // no zero-threshold test on v: a visited candidate is a

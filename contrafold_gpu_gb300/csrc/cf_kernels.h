@@ -47,9 +47,6 @@ FoldKernels fold_kernels(bool wide);
 // k_fold_cluster32: one group folded by the kClusterCtas CTAs of a cluster
 // (grid = groups x kClusterCtas, kFoldThreads per CTA)
 constexpr int kClusterCtas = 8;
-#ifndef CF_CLUSTER_ROW_PF
-#define CF_CLUSTER_ROW_PF 1   // window-walk loads in flight per lane in the cluster kernels
-#endif
 #ifndef CF_CLUSTER_CHAIN_PF
 #define CF_CLUSTER_CHAIN_PF 8   // bifurcation-chain pipeline depth in the cluster kernels
 #endif

@@ -206,7 +206,6 @@ __device__ __forceinline__ void outside_A_merged(const Lse32& sr, const SmemTabs
 // `lanes`: the lanes evaluating cells together, walked in lockstep as in
 // inside_B (rows from the largest l1max among them, per row as many slots as
 // the lane with the most candidates).
-template <int PF = 1>
 __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>* __restrict__ tb,
                                           const SeqV& Q, const OutTabs& T, int a, int b, unsigned lanes) {
     const ParamView<float> P{tb->blob};
@@ -267,7 +266,7 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
         const int slots = __reduce_max_sync(lanes, __popc(msk));
         float sn0, sn1;
         snuc_row(l1, sn0, sn1);
-        lockstep_row<true, PF, float>(
+        lockstep_row<true, float>(
             msk, slots, [&](int bit) { return src_val(l1, b + 1 + bit); },
             [&](int bit, float v) { source(l1, b + 1 + bit, v, sn0, sn1); });
     }
@@ -290,7 +289,6 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
 // term comes last.  Returns the clipped value.
 // `lanes`: the lanes evaluating pairs together, walked in lockstep as in
 // inside_B.
-template <int PF = 1>
 __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restrict__ tb, const PolyTables* pt,
                                                 const SeqV& Q, const OutTabs& T, float Z, int a, int b,
                                                 unsigned lanes) {
@@ -357,7 +355,7 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
         const int slots = __reduce_max_sync(lanes, __popc(msk));
         float sn0, sn1;
         snuc_row(l1, sn0, sn1);
-        lockstep_row<false, PF, float>(
+        lockstep_row<false, float>(
             msk, slots, [&](int bit) { return src_val(l1, b + bit); },
             [&](int bit, float v) { source(l1, b + bit, v, sn0, sn1); });
     }
