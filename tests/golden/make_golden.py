@@ -25,6 +25,11 @@ writes tests/golden/exhaustive.json.gz instead: every ACGU sequence of 1-5 nt
 without a mask and every (sequence, mask) pair of 1-4 nt, each with FP64 logZ,
 the Viterbi and MEA (gamma 6) structures and the first 16 hex digits of the
 SHA-256 of its float32 posterior matrix.
+
+    python tests/golden/make_golden.py --long
+writes tests/golden/long.json: seven seeded sequences of 300-600 nt (masks
+Bernoulli 0.1 / 0.3 on some, N on one) with the same fields as golden.json
+(minutes per case: the reference runs as plain Python).
 """
 from __future__ import annotations
 
@@ -142,6 +147,17 @@ def exhaustive_cases():
     return cases
 
 
+def long_cases():
+    rng = np.random.default_rng(20261203)
+    out = []
+    for L, p, alpha in ((300, 0.1, "ACGU"), (350, 0.0, "ACGU"), (400, 0.1, "ACGU"), (450, 0.3, "ACGUN"),
+                        (500, 0.1, "ACGU"), (600, 0.1, "ACGU"), (600, 0.0, "ACGU")):
+        seq = rand_seq(rng, L, alpha)
+        mask = (rng.random(L) < p).astype(np.int8).tolist() if p > 0 else None
+        out.append((seq, mask, [6.0], False))
+    return out
+
+
 def rand_seq(rng, L, alphabet="ACGU"):
     return "".join(rng.choice(np.array(list(alphabet)), size=L))
 
@@ -198,7 +214,24 @@ def main():
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--out", default=None)
     ap.add_argument("--exhaustive", action="store_true", help="all short sequences (and masks): exhaustive.json.gz")
+    ap.add_argument("--long", action="store_true", help="seven 300-600 nt sequences: long.json")
     args = ap.parse_args()
+    if args.long:
+        cases = long_cases()
+        t0 = time.time()
+        with mp.get_context("spawn").Pool(min(args.jobs, len(cases)), initializer=_init, initargs=(args.ref,)) as pool:
+            order = sorted(range(len(cases)), key=lambda k: -len(cases[k][0]))
+            res = pool.map(_run_case, [cases[k] for k in order], chunksize=1)
+        recs = [None] * len(cases)
+        for k, r in zip(order, res):
+            recs[k] = r
+        out = args.out or os.path.join(HERE, "long.json")
+        with open(out, "w") as fh:
+            json.dump({"generator": "tests/golden/make_golden.py --long",
+                       "reference": "gpu_contrafold/cpu.py (pure Python under an identity numba.njit)",
+                       "cases": recs}, fh, indent=0)
+        print(f"wrote {len(recs)} cases to {out} in {time.time() - t0:.0f}s")
+        return
     if args.exhaustive:
         cases = exhaustive_cases()
         t0 = time.time()
