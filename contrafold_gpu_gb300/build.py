@@ -4,6 +4,12 @@ Every translation unit in csrc/ is compiled for sm_103a only, in parallel,
 then linked into one shared library that exports the C-ABI of
 include/contrafold_gb300.h.  `-fmad=false` keeps every float add and multiply
 separately rounded (the FP32 paths are bitwise parity targets).
+
+`--check` (build(check=True)) builds the same sources with -DCF_CHECK into
+libcontrafold_gb300_check.so: every DP-table subscript of the fold kernels is
+checked against its table's size and reported with printf instead of being
+performed out of range.  Point the package at it with the environment
+variable CONTRAFOLD_GB300_LIB to run the test suite against it.
 """
 from __future__ import annotations
 
@@ -17,6 +23,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libcontrafold_gb300.so")
+LIB_CHECK = os.path.join(HERE, "libcontrafold_gb300_check.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -40,23 +47,29 @@ def _deps():
         [os.path.join(os.path.dirname(HERE), "include", "contrafold_gb300.h")]
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, check: bool = False) -> str:
+    """Compile and link the library (the checked variant with check=True);
+    returns its path.  Skips the work when the library is newer than every
+    source."""
+    lib = LIB_CHECK if check else LIB
+    if not force and up_to_date(lib):
+        return lib
+    bdir = BUILD_DIR + ("_check" if check else "")
+    os.makedirs(bdir, exist_ok=True)
     cc = nvcc()
     srcs = _sources()
+    flags = NVCC_FLAGS + (["-DCF_CHECK"] if check else [])
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.basename(src).replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        obj = os.path.join(bdir, os.path.basename(src).replace(".cu", ".o"))
+        cmd = [cc, *ARCH, *flags, "-c", src, "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,14 +81,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with cfut.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, check="--check" in sys.argv))

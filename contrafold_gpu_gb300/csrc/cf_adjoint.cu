@@ -59,9 +59,11 @@ __device__ __forceinline__ AdjView adj_view(const FoldArgs& A, const SeqDesc& D)
     AdjView V;
     V.I.FC = base + r.a.FC; V.I.FM = base + r.a.FM; V.I.FM1 = base + r.a.FM1; V.I.F5 = base + r.a.F5;
     V.I.m = D.L + 1;
+    V.I.sized(D.L);
     V.O.FC = V.I.FC; V.O.FM = V.I.FM; V.O.FM1 = V.I.FM1; V.O.F5 = V.I.F5;
     V.O.FCo = base + r.a.FCo; V.O.FMo = base + r.a.FMo; V.O.FM1o = base + r.a.FM1o; V.O.FM2o = base + r.a.FM2o;
     V.O.F5o = base + r.a.F5o; V.O.m = D.L + 1;
+    V.O.sized(D.L);
     V.FM2 = base + r.FM2;
     V.U = reinterpret_cast<const double*>(base + r.U);
     V.UD = reinterpret_cast<double*>(base + r.UD);

@@ -9,6 +9,9 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#ifdef CF_CHECK
+#include <cstdio>
+#endif
 
 #include "../../include/contrafold_gb300.h"
 
@@ -44,6 +47,46 @@ __host__ __device__ __forceinline__ int64_t tri_size(int L) {
 // below 2^31 for d <= 32,768, so the halving is a shift (no signed-division
 // rounding fix-up).
 __host__ __device__ __forceinline__ int tri_off(int d, int m) { return d * m - ((d * (d - 1)) >> 1); }
+
+// ---------------------------------------------------------------------------
+// Checked table access (debug builds: -DCF_CHECK, build.py --check).  The DP
+// table pointers of the views (InTabs, OutTabs) become TabPtr, whose
+// subscript and offset check the cell index against the table's size (set by
+// the views' sized(L)); an index outside it is reported with printf (the first
+// 16 per module) and replaced by 0, so the access stays inside the table and
+// the kernel goes on -- no trap, no fault.  In normal builds CF_TAB(R) is R*
+// and sized() is empty: the generated code is unchanged.
+// ---------------------------------------------------------------------------
+#ifdef CF_CHECK
+static __device__ unsigned cf_check_hits;   // violations seen by this module's kernels
+
+__device__ __forceinline__ int64_t cf_checked_index(int64_t i, int64_t n) {
+    if (i >= 0 && i < n) return i;
+    if (atomicAdd(&cf_check_hits, 1u) < 16u)
+        printf("cf_check: block %d thread %d: cell %lld outside a table of %lld cells\n", (int)blockIdx.x,
+               (int)threadIdx.x, (long long)i, (long long)n);
+    return 0;
+}
+
+template <typename R>
+struct TabPtr {
+    R* p = nullptr;
+    int64_t n = INT64_MAX;   // cells; unchecked until sized
+    TabPtr() = default;
+    __host__ __device__ TabPtr(R* q) : p(q) {}
+    template <typename Q>
+    __host__ __device__ TabPtr(const TabPtr<Q>& o) : p(o.p), n(o.n) {}
+    __device__ R& operator[](int i) const { return p[cf_checked_index(i, n)]; }
+    __device__ R& operator[](int64_t i) const { return p[cf_checked_index(i, n)]; }
+    __device__ R* operator+(int o) const { return p + cf_checked_index(o, n); }
+    __device__ operator R*() const { return p; }
+};
+#define CF_TAB(R) ::cf::TabPtr<R>
+#define CF_SIZE_TAB(t, cells) ((t).n = (int64_t)(cells))
+#else
+#define CF_TAB(R) R*
+#define CF_SIZE_TAB(t, cells) ((void)0)
+#endif
 
 // Round a word count up to 32 words (128 bytes).
 __host__ __device__ __forceinline__ int64_t pad32(int64_t w) { return (w + 31) & ~int64_t(31); }

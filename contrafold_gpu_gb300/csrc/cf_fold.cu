@@ -165,6 +165,7 @@ __device__ __forceinline__ InView<R> in_view(const FoldArgs& A, int64_t ws_off, 
         V.PLs = plist_at(A.ws + ws_off + a.PL, L);
     }
     V.T.m = L + 1;
+    V.T.sized(L);
     V.fbs = (int)pad32(L + 2);
     return V;
 }
@@ -177,6 +178,7 @@ __device__ __forceinline__ OutTabs out_tabs(const FoldArgs& A, int64_t ws_off, i
     T.FCo = base + a.FCo; T.FMo = base + a.FMo; T.FM1o = base + a.FM1o; T.FM2o = base + a.FM2o;
     T.F5o = base + a.F5o;
     T.m = L + 1;
+    T.sized(L);
     return T;
 }
 

@@ -79,12 +79,20 @@ __device__ __forceinline__ void load_tabs(SmemTabs<R>* t, const R* __restrict__ 
 // Inside tables of one sequence, triangular diagonal-major (see cf_device.cuh).
 template <typename R>
 struct InTabs {
-    R* FC;
-    R* FM;
-    R* FM1;
-    R* F5;
+    CF_TAB(R) FC;
+    CF_TAB(R) FM;
+    CF_TAB(R) FM1;
+    CF_TAB(R) F5;
     int m;   // L + 1
     __device__ __forceinline__ int at(int i, int j) const { return tri_off(j - i, m) + i; }
+    // table sizes for checked builds (nothing otherwise)
+    __device__ __forceinline__ void sized(int L) {
+        CF_SIZE_TAB(FC, tri_size(L));
+        CF_SIZE_TAB(FM, tri_size(L));
+        CF_SIZE_TAB(FM1, tri_size(L));
+        CF_SIZE_TAB(F5, L + 2);
+        (void)L;
+    }
 };
 
 // ScoreJunctionA(i, j) for the pair (i, j+1) (cpu.py:224-228).

@@ -24,17 +24,30 @@
 namespace cf {
 
 struct OutTabs {
-    const float* FC;
-    const float* FM;
-    const float* FM1;
-    const float* F5;
-    float* FCo;
-    float* FMo;
-    float* FM1o;
-    float* FM2o;
-    float* F5o;
+    CF_TAB(const float) FC;
+    CF_TAB(const float) FM;
+    CF_TAB(const float) FM1;
+    CF_TAB(const float) F5;
+    CF_TAB(float) FCo;
+    CF_TAB(float) FMo;
+    CF_TAB(float) FM1o;
+    CF_TAB(float) FM2o;
+    CF_TAB(float) F5o;
     int m;
     __device__ __forceinline__ int at(int i, int j) const { return tri_off(j - i, m) + i; }
+    // table sizes for checked builds (nothing otherwise)
+    __device__ __forceinline__ void sized(int L) {
+        CF_SIZE_TAB(FC, tri_size(L));
+        CF_SIZE_TAB(FM, tri_size(L));
+        CF_SIZE_TAB(FM1, tri_size(L));
+        CF_SIZE_TAB(F5, L + 2);
+        CF_SIZE_TAB(FCo, tri_size(L));
+        CF_SIZE_TAB(FMo, tri_size(L));
+        CF_SIZE_TAB(FM1o, tri_size(L));
+        CF_SIZE_TAB(FM2o, tri_size(L));
+        CF_SIZE_TAB(F5o, L + 2);
+        (void)L;
+    }
 };
 
 // F5o (cpu.py:684-699) by one warp, k = L-1 .. 0.  Target k receives, in the

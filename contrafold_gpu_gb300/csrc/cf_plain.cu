@@ -311,6 +311,7 @@ __device__ __forceinline__ OutTabs plain_out(const FoldArgs& A, const SeqDesc& D
     T.FCo = base + a.FCo; T.FMo = base + a.FMo; T.FM1o = base + a.FM1o; T.FM2o = base + a.FM2o;
     T.F5o = base + a.F5o;
     T.m = D.L + 1;
+    T.sized(D.L);
     return T;
 }
 
@@ -326,6 +327,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_plain_inside32(FoldArgs A) {
     float* base = A.ws + D.ws_off;
     InTabs<float> T;
     T.FC = base + ar.FC; T.FM = base + ar.FM; T.FM1 = base + ar.FM1; T.F5 = base + ar.F5; T.m = D.L + 1;
+    T.sized(D.L);
     for (int d = 0; d <= D.L; ++d) {
         for (int i = threadIdx.x; i + d <= D.L; i += blockDim.x) plain_inside_cell<Lse32>(sr, &sm->tabs, Q, T, i, i + d);
         __syncthreads();

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(kSampleWarps * 32) k_sample32(SampleArgs A) {
         float* base = A.ws + D.ws_off;
         X.T.FC = base + ar.FC; X.T.FM = base + ar.FM; X.T.FM1 = base + ar.FM1; X.T.F5 = base + ar.F5;
         X.T.m = L + 1;
+        X.T.sized(L);
         if (A.seeds != nullptr) {
             const uint64_t sd = A.seeds[D.idx];
             sample_one(X, smp, 0, make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), out, stack, A.status, lane);

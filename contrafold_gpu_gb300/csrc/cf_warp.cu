@@ -99,6 +99,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
     const Arena32 ar = arena32(L);
     InTabs<float> T;
     T.FC = base + ar.FC; T.FM = base + ar.FM; T.FM1 = base + ar.FM1; T.F5 = base + ar.F5; T.m = m;
+    T.sized(L);
     float* FB = base + ar.FB;
     const int fbs = (int)pad32(L + 2);
     const PairList PLs = plist_at(base + ar.PL, L);
@@ -157,6 +158,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
     O.FC = T.FC; O.FM = T.FM; O.FM1 = T.FM1; O.F5 = T.F5;
     O.FCo = base + ar.FCo; O.FMo = base + ar.FMo; O.FM1o = base + ar.FM1o; O.FM2o = base + ar.FM2o;
     O.F5o = base + ar.F5o; O.m = m;
+    O.sized(L);
     exterior_outside_warp(sr, &sm->tabs, Q, O);
     for (int t = L; t >= 0; --t) {
         const int dB = t - 1;

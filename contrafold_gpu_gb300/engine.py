@@ -15,7 +15,9 @@ import numpy as np
 from . import params as _params
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libcontrafold_gb300.so")
+# CONTRAFOLD_GB300_LIB selects another build of the library (the checked one
+# of build.py --check); the default is the in-tree release build
+LIB_PATH = os.environ.get("CONTRAFOLD_GB300_LIB") or os.path.join(HERE, "libcontrafold_gb300.so")
 
 CF_OK, CF_EINVAL, CF_ENOMEM, CF_ETIMEOUT, CF_ECUDA, CF_EDEVICE, CF_ECANCELLED = 0, 1, 2, 3, 4, 5, 6
 CF_MAX_LEN = 32767

@@ -75,3 +75,13 @@ def test_params_loader_tying(P):
     b32 = params.pack32(P)
     assert b32.dtype == np.float32 and b32.size == params.BLOB_LEN
     assert b32[params.OFFSETS["mu"]] == np.float32(P["mu"])
+
+
+def test_checked_build_compiles_and_exports_every_symbol():
+    """build.py --check: the same sources with per-subscript table checks
+    (-DCF_CHECK) compile and export the whole C-ABI (no GPU needed)."""
+    from contrafold_gpu_gb300 import build
+    lib = build.build(check=True)
+    assert lib.endswith("libcontrafold_gb300_check.so")
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+    assert set(header_symbols()) <= set(re.findall(r" T (cf_\w+)", out))
