@@ -30,6 +30,10 @@ SHA-256 of its float32 posterior matrix.
 writes tests/golden/long.json: seven seeded sequences of 300-600 nt (masks
 Bernoulli 0.1 / 0.3 on some, N on one) with the same fields as golden.json
 (minutes per case: the reference runs as plain Python).
+
+    python tests/golden/make_golden.py --xlong
+writes tests/golden/xlong.json: one 800-nt and one 1,000-nt sequence (the
+latter with a Bernoulli 0.1 mask), about an hour of pure Python.
 """
 from __future__ import annotations
 
@@ -158,6 +162,14 @@ def long_cases():
     return out
 
 
+def xlong_cases():
+    rng = np.random.default_rng(20261204)
+    s800 = rand_seq(rng, 800)
+    s1000 = rand_seq(rng, 1000)
+    m1000 = (rng.random(1000) < 0.1).astype(np.int8).tolist()
+    return [(s800, None, [6.0], False), (s1000, m1000, [6.0], False)]
+
+
 def rand_seq(rng, L, alphabet="ACGU"):
     return "".join(rng.choice(np.array(list(alphabet)), size=L))
 
@@ -215,9 +227,10 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--exhaustive", action="store_true", help="all short sequences (and masks): exhaustive.json.gz")
     ap.add_argument("--long", action="store_true", help="seven 300-600 nt sequences: long.json")
+    ap.add_argument("--xlong", action="store_true", help="800 and 1,000 nt sequences: xlong.json")
     args = ap.parse_args()
-    if args.long:
-        cases = long_cases()
+    if args.long or args.xlong:
+        cases = long_cases() if args.long else xlong_cases()
         t0 = time.time()
         with mp.get_context("spawn").Pool(min(args.jobs, len(cases)), initializer=_init, initargs=(args.ref,)) as pool:
             order = sorted(range(len(cases)), key=lambda k: -len(cases[k][0]))
@@ -225,9 +238,9 @@ def main():
         recs = [None] * len(cases)
         for k, r in zip(order, res):
             recs[k] = r
-        out = args.out or os.path.join(HERE, "long.json")
+        out = args.out or os.path.join(HERE, "long.json" if args.long else "xlong.json")
         with open(out, "w") as fh:
-            json.dump({"generator": "tests/golden/make_golden.py --long",
+            json.dump({"generator": "tests/golden/make_golden.py " + ("--long" if args.long else "--xlong"),
                        "reference": "gpu_contrafold/cpu.py (pure Python under an identity numba.njit)",
                        "cases": recs}, fh, indent=0)
         print(f"wrote {len(recs)} cases to {out} in {time.time() - t0:.0f}s")
