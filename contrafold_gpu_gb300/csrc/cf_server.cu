@@ -374,16 +374,21 @@ int cf_server_submit(cf_server* S, const cf_request* r, const uint8_t* seq, int3
 int cf_server_wait(cf_server* S, int64_t ticket, int32_t timeout_ms, float* logz_out, char* out, int64_t out_cap) {
     if (!S) return fail(CF_EINVAL, "server is NULL");
     std::unique_lock<std::mutex> lk(S->mu);
-    auto it = S->reqs.find(ticket);
-    if (it == S->reqs.end()) return fail(CF_EINVAL, "unknown ticket");
-    Req* q = it->second.get();
-    auto ready = [&] { return q->state == kDone; };
+    if (S->reqs.find(ticket) == S->reqs.end()) return fail(CF_EINVAL, "unknown ticket");
+    // the request is looked up on every wake-up: another wait on the same
+    // ticket may have collected (and freed) it meanwhile
+    auto ready = [&] {
+        auto f = S->reqs.find(ticket);
+        return f == S->reqs.end() || f->second->state == kDone;
+    };
     if (timeout_ms < 0) {
         S->cv_done.wait(lk, ready);
     } else if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
         return fail(CF_ETIMEOUT, "request not finished within the timeout");
     }
-    return collect(S, S->reqs.find(ticket), logz_out, out, out_cap, nullptr, q->t_submit);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return fail(CF_EINVAL, "ticket collected by another wait");
+    return collect(S, it, logz_out, out, out_cap, nullptr, it->second->t_submit);
 }
 
 int cf_server_cancel(cf_server* S, int64_t ticket) {
@@ -440,9 +445,16 @@ int cf_server_replay(cf_server* S, int32_t n, const double* t_arrive, const cf_r
     int first_rc = CF_OK;
     for (int k = 0; k < n; ++k) {
         std::unique_lock<std::mutex> lk(S->mu);
-        auto it = S->reqs.find(tickets[k]);
-        Req* q = it->second.get();
-        S->cv_done.wait(lk, [&] { return q->state == kDone; });
+        const int64_t tk = tickets[k];
+        S->cv_done.wait(lk, [&] {
+            auto f = S->reqs.find(tk);
+            return f == S->reqs.end() || f->second->state == kDone;
+        });
+        auto it = S->reqs.find(tk);
+        if (it == S->reqs.end()) {   // collected by a wait on the same ticket
+            status_out[k] = CF_EINVAL;
+            continue;
+        }
         const int64_t L = offsets[k + 1] - offsets[k];
         const int64_t cap = reqs[k].op == CF_OP_SAMPLE ? L * reqs[k].n_samples : L;
         const int rc = collect(S, it, reqs[k].op == CF_OP_LOGZ ? logz_out + k : nullptr,

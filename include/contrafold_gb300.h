@@ -252,7 +252,9 @@ int cf_server_submit(cf_server* server, const cf_request* req, const uint8_t* se
 /* Blocks until the request is done (timeout_ms < 0: no limit; on expiry
  * CF_ETIMEOUT and the request stays), then returns its status and outputs and
  * forgets the ticket: logZ in *logz_out, or the dot-bracket (L bytes) or the
- * samples (n_samples * L bytes, sample-major) in out[0 .. out_cap). */
+ * samples (n_samples * L bytes, sample-major) in out[0 .. out_cap).  Of
+ * several threads waiting on one ticket, one gets the outputs, the others
+ * CF_EINVAL. */
 int cf_server_wait(cf_server* server, int64_t ticket, int32_t timeout_ms,
                    float* logz_out, char* out, int64_t out_cap);
 /* A request still queued is dropped; its wait returns CF_ECANCELLED. */
