@@ -15,7 +15,8 @@
 // above long_len are "long", and only the first long_workers workers take long
 // batches (they take short ones when no long request waits); the others serve
 // short buckets only.  The engine picks the kernels per batch (small batches
-// fold one sequence per CTA, the latency-optimal shape).
+// fold one sequence per CTA, or per 8-SM thread-block cluster when every
+// sequence has 512 nt or more -- the latency-optimal shapes).
 //
 // Every result is what the same request gives alone: logZ and MEA do not
 // depend on batch composition, and samples use a per-request seed
