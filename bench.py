@@ -48,10 +48,8 @@ UNIT = "folds/s"
 
 
 def workload(n: int, L: int, p_mask: float = 0.1):
-    idx = np.random.default_rng(0).integers(0, 4, size=(n, L), dtype=np.int8)
-    seq_bytes = np.frombuffer(b"ACGU", np.uint8)[idx]                       # (n, L) ASCII
-    mask = (np.random.default_rng(1).random((n, L)) < p_mask).astype(np.uint8)
-    return seq_bytes, mask
+    from contrafold_gpu_gb300 import workloads
+    return workloads.mea_200(n, L, p_mask)
 
 
 def dist_env():
@@ -392,6 +390,142 @@ def our_arm(args):
     return 0
 
 
+def decoder_arm(args):
+    """The other two decoders of the 10,000 x 200 nt workload (same sequences and
+    Bernoulli(0.1) masks as the headline), one JSON line each:
+      bpp : base-pair posterior matrices (inside + outside + posterior, float32,
+            bitwise the reference's), packed L x L float32 per sequence;
+      mfe : Viterbi structures (FP64 max-plus inside + EPS first-match traceback).
+    value: device-resident plan, CUDA events on the launch stream, L2 flushed
+    between steps; e2e: the public batch call (bpp_batch / mfe_batch) with
+    Python strings in and results out; cpu_baseline: the oracle on all host
+    cores over a bounded sample."""
+    import torch
+    import contrafold_gpu_gb300 as cg
+    from contrafold_gpu_gb300 import build as cbuild
+    from contrafold_gpu_gb300.engine import CF_JOB_BPP, CF_JOB_MFE, Engine, Plan
+    from oracle import oracle as O
+    cbuild.build()
+    P = cg.load()
+    n, L = args.n, args.L
+    seq_bytes, mask = workload(n, L)
+    offsets = np.arange(n + 1, dtype=np.int64) * L
+    dev = torch.device("cuda", 0)
+    d_seqs = torch.from_numpy(seq_bytes.reshape(-1).copy()).to(dev)
+    d_mask = torch.from_numpy(mask.reshape(-1).copy()).to(dev)
+    bpp = args.workload == "bpp"
+    d_out = (torch.empty(n * L * L, dtype=torch.float32, device=dev) if bpp
+             else torch.empty(n * L, dtype=torch.uint8, device=dev))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(dev)
+
+    def run_mode(mode, clk=None):
+        eng = Engine(P, mode=mode)
+        plan = Plan(eng, CF_JOB_BPP if bpp else CF_JOB_MFE, offsets)
+        for _ in range(args.warmup):
+            plan.run(d_seqs.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+        plan.status()
+        ms = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(d_seqs.data_ptr(), d_mask.data_ptr(), d_out.data_ptr(), 6.0, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+        plan.status()
+        res = {"ms": ms, "launches": plan.launches * args.steps, "schedule": plan.schedule, "group": plan.group}
+        plan.close()
+        eng.close()
+        return res
+
+    plain = run_mode("plain")
+    with ClockSampler(0) as clk:
+        batched = run_mode("batched")
+    clocks = clk.summary()
+    value = n * len(batched["ms"]) / (sum(batched["ms"]) / 1e3)
+    seqs = [bytes(r).decode() for r in seq_bytes]
+    masks = list(mask)
+    # e2e through the public API
+    api = cg.gpu.bpp_batch if bpp else cg.gpu.mfe_batch
+    api(seqs[:256], P, masks[:256])
+    t0 = time.perf_counter()
+    k_e2e = max(1, min(args.steps, 3))
+    for _ in range(k_e2e):
+        res = api(seqs, P, masks)
+    e2e = n * k_e2e / (time.perf_counter() - t0)
+    # device result vs the public call (first 64 sequences)
+    if bpp:
+        dev_mats = d_out[: 64 * L * L].cpu().numpy().reshape(64, L, L)
+        same = all(np.array_equal(dev_mats[b].astype(np.float64), res[b]) for b in range(64))
+    else:
+        st = d_out[: 64 * L].cpu().numpy().tobytes().decode("ascii")
+        same = all(st[b * L:(b + 1) * L] == res[b] for b in range(64))
+    # CPU baseline (the oracle on all host cores, bounded sample) and op counts
+    O.build()
+    cores = os.cpu_count() or 1
+    job = O.JOB_LOGZ32 if bpp else O.JOB_MFE     # JOB_LOGZ32 runs the whole float32 posterior
+    done, tt = 0, 0.0
+    while done < n and tt < 12.0:
+        sl = slice(done, min(n, done + 4 * cores))
+        t0 = time.perf_counter()
+        O.batch(job, seqs[sl], P, masks[sl], 6.0, threads=cores)
+        tt += time.perf_counter() - t0
+        done = sl.stop
+    cnt = np.zeros(8)
+    for b in range(32):
+        cnt += O.count_mea_ops(seqs[b], P, masks[b], 6.0)
+    cnt /= 32
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = float(measured_peaks().get("sm_max_mhz", 2070.0))
+    t_step = statistics.mean(batched["ms"]) / 1e3
+    if bpp:
+        ops = float(sum(cnt[c] * O.OP_COST[c] for c in range(7)))
+        peak = props.multi_processor_count * 128 * sm_mhz * 1e6 / 1e12
+        roof = {"bound": "fp32", "unit": "TFLOP/s", "ops_per_fold": ops,
+                "peak_note": f"{props.multi_processor_count} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (derived, "
+                             "sm_max_mhz of MEASURED_PEAKS.json; no measured FP32 peak there)"}
+    else:
+        ops = float(sum(cnt[c] * O.VITERBI_COST[c] for c in range(3)))
+        peak = 1.25   # nominal GB300 FP64 rate (TFLOP/s): 2 DFMA lanes x 2 FLOP per SM per clock
+        roof = {"bound": "fp64", "unit": "TFLOP/s (FP64 lane-ops counted as DFMA-equivalent FLOP: x2)",
+                "ops_per_fold": ops,
+                "peak_note": "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak); each FP64 add or compare "
+                             "occupies one DFMA slot, so achieved = 2 x FP64 ops / s"}
+    achieved = (ops * n / t_step / 1e12) * (1 if bpp else 2)
+    roof.update({"kernel": ("k_fold_group32<BPP>" if batched["schedule"] == "group" else batched["schedule"])
+                 if bpp else "k_viterbi64", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+                 "traffic": None})
+    out_bytes = n * L * L * 4 if bpp else n * L
+    line = {"metric": ("200-nt BPP folds/s" if bpp else "200-nt Viterbi (MFE) folds/s") + " on 1 GB300",
+            "value": value, "unit": "folds/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(batched["ms"]), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if bpp else "f64", "data": "synthetic",
+            "config": {"workload": ("BPP (inside+outside+posterior, float32 L x L per sequence)" if bpp else
+                                    "Viterbi (FP64 max-plus + EPS=1e-6 first-match traceback)") +
+                                   f", {n} x {L} nt i.i.d. ACGU, Bernoulli(0.1) forced-unpaired mask",
+                       "n_seqs": n, "seq_len": L, "mask_p": 0.1, "schedule": batched["schedule"],
+                       "group": batched["group"], "l2": "flushed between steps (256 MiB write)"},
+            "plain": {"value": n * len(plain["ms"]) / (sum(plain["ms"]) / 1e3),
+                      "ms_per_step": statistics.mean(plain["ms"])},
+            "batched_vs_plain": statistics.mean(plain["ms"]) / statistics.mean(batched["ms"]),
+            "gpu_launches": batched["launches"],
+            "e2e": {"value": e2e, "unit": "folds/s", "api": "contrafold_gpu_gb300.gpu." + api.__name__,
+                    "h2d_bytes_per_step": int(2 * n * L + 8 * (n + 1) + 24 * n), "d2h_bytes_per_step": out_bytes,
+                    "matches_device_path": bool(same)},
+            "roofline": roof,
+            "cpu_baseline": {"value": done / tt, "unit": "folds/s", "cores": cores, "kind": "port",
+                             "sample": f"first {done} sequences of the workload, {cores} threads, {tt:.1f} s "
+                                       + ("(float32 posterior, cpu.py:583-820 restated)" if bpp else
+                                          "(FP64 Viterbi + traceback, cpu.py:290-519 restated)")},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def serving_arm(args):
     """Open-loop serving sweep: saturated throughput (every request queued at
     t = 0), then Poisson streams at fractions of it; p50 / p99 latency from the
@@ -621,9 +755,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=10000)
     ap.add_argument("--L", type=int, default=200)
-    ap.add_argument("--workload", choices=["mea", "serving", "logz", "sampling", "grad"], default="mea",
-                    help="mea: the headline 200-nt MEA batch; serving: the open-loop request-stream sweep; "
-                         "logz / sampling / grad: the other measured workloads")
+    ap.add_argument("--workload", choices=["mea", "bpp", "mfe", "serving", "logz", "sampling", "grad"], default="mea",
+                    help="mea: the headline 200-nt MEA batch; bpp / mfe: the other decoders of the same "
+                         "batch; serving: the open-loop request-stream sweep; logz / sampling / grad: the other "
+                         "measured workloads")
     ap.add_argument("--workers", type=int, default=6, help="serving: engines / worker threads")
     ap.add_argument("--long-workers", type=int, default=2, help="serving: workers that take long requests")
     ap.add_argument("--long-len", type=int, default=256, help="serving: buckets above this length are long")
@@ -637,6 +772,8 @@ def main():
         return serving_arm(args)
     if args.workload in ("logz", "sampling", "grad"):
         return side_arm(args)
+    if args.workload in ("bpp", "mfe"):
+        return decoder_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return our_arm(args)

@@ -910,6 +910,7 @@ struct cf_plan {
     DevBuf<SeqDesc> descs;
     DevBuf<float> arena;
     DevBuf<int> status;
+    DevBuf<int64_t> post_offs;   // CF_JOB_BPP: sequence b's matrix at sum_{c<b} L_c^2 floats
     PhaseTimer timer;
     int launches = 0;
     // CUDA graph of the plan's launches, replayed while the run arguments stay
@@ -949,12 +950,13 @@ int cf_plan_create(cf_engine* e, int32_t job, const int64_t* offsets, int32_t n,
     *out = nullptr;
     int rc = check_batch(e, reinterpret_cast<const uint8_t*>(1), offsets, n);
     if (rc) return rc;
-    if (job != CF_JOB_LOGZ && job != CF_JOB_LOGZ64 && job != CF_JOB_MEA && job != CF_JOB_MFE)
-        return fail(CF_EINVAL, "plans support CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_MEA, CF_JOB_MFE");
+    if (job != CF_JOB_LOGZ && job != CF_JOB_LOGZ64 && job != CF_JOB_BPP && job != CF_JOB_MEA && job != CF_JOB_MFE)
+        return fail(CF_EINVAL, "plans support CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_BPP, CF_JOB_MEA, CF_JOB_MFE");
     CF_CUDA(cudaSetDevice(e->device));
     cf_plan* p = new cf_plan();
     p->eng = e;
-    p->job = job == CF_JOB_LOGZ ? JOB_LOGZ : job == CF_JOB_LOGZ64 ? JOB_LOGZ64 : job == CF_JOB_MEA ? JOB_MEA : JOB_MFE;
+    p->job = job == CF_JOB_LOGZ ? JOB_LOGZ : job == CF_JOB_LOGZ64 ? JOB_LOGZ64 : job == CF_JOB_BPP ? JOB_BPP
+           : job == CF_JOB_MEA ? JOB_MEA : JOB_MFE;
     p->n = n;
     if ((rc = make_plan(e, p->job, offsets, n, p->P)) || (rc = p->descs.ensure(std::max(n, 1))) ||
         (rc = p->status.ensure(2))) {
@@ -969,6 +971,19 @@ int cf_plan_create(cf_engine* e, int32_t job, const int64_t* offsets, int32_t n,
         return rc;
     }
     if (n) CF_CUDA(cudaMemcpy(p->descs.p, p->P.descs.data(), sizeof(SeqDesc) * n, cudaMemcpyHostToDevice));
+    if (p->job == JOB_BPP) {
+        std::vector<int64_t> po(std::max(n, 1), 0);
+        int64_t acc = 0;
+        for (int b = 0; b < n; ++b) {
+            po[b] = acc;
+            acc += (offsets[b + 1] - offsets[b]) * (offsets[b + 1] - offsets[b]);
+        }
+        if ((rc = p->post_offs.ensure(po.size()))) {
+            cf_plan_destroy(p);
+            return rc;
+        }
+        CF_CUDA(cudaMemcpy(p->post_offs.p, po.data(), sizeof(int64_t) * po.size(), cudaMemcpyHostToDevice));
+    }
     CF_CUDA(cudaMemset(p->status.p, 0, sizeof(int)));
     *out = p;
     return CF_OK;
@@ -979,7 +994,7 @@ int cf_plan_destroy(cf_plan* p) {
     cudaSetDevice(p->eng->device);
     cudaDeviceSynchronize();
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
-    p->descs.release(); p->arena.release(); p->status.release();
+    p->descs.release(); p->arena.release(); p->status.release(); p->post_offs.release();
     delete p;
     return CF_OK;
 }
@@ -999,6 +1014,8 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
     float* lz = p->job == JOB_LOGZ ? static_cast<float*>(d_out) : nullptr;
     double* lz64 = p->job == JOB_LOGZ64 ? static_cast<double*>(d_out) : nullptr;
     char* st_out = (p->job == JOB_MEA || p->job == JOB_MFE) ? static_cast<char*>(d_out) : nullptr;
+    float* post = p->job == JOB_BPP ? static_cast<float*>(d_out) : nullptr;
+    const int64_t* post_offs = p->job == JOB_BPP ? p->post_offs.p : nullptr;
     if (p->graph_on && !p->timer.on && p->n > 0) {
         const bool hit = p->gexec != nullptr && p->g_seqs == d_seqs && p->g_mask == d_mask && p->g_out == d_out &&
                          p->g_gamma == gamma;
@@ -1011,7 +1028,7 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
             }
             CF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             X.timer = nullptr;
-            rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
+            rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, post, post_offs, st);
             cudaGraph_t g = nullptr;
             const cudaError_t ec = cudaStreamEndCapture(st, &g);
             if (rc || ec != cudaSuccess) {
@@ -1034,7 +1051,7 @@ int cf_plan_run(cf_plan* p, const uint8_t* d_seqs, const uint8_t* d_mask, float 
         p->launches = p->g_launches;
         return CF_OK;
     }
-    int rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, nullptr, nullptr, st);
+    int rc = run_device(p->eng, p->job, p->P, X, d_seqs, d_mask, gamma, lz, lz64, st_out, post, post_offs, st);
     p->launches = X.launches;
     return rc;
 }

@@ -110,6 +110,20 @@ __global__ void k_scratch_descs(const int64_t* __restrict__ offs, int n, cf::Seq
         }                                                                                 \
     } while (0)
 
+// The same for calls made once work is queued on `st`: the stream is drained
+// (its own error ignored) before the failure is returned, so the lock is
+// released only when nothing of this call can still write the scratch.
+#define CF_CUDA_Q(call)                                                                   \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            char m_[256];                                                                 \
+            std::snprintf(m_, sizeof m_, "%s: %s", #call, cudaGetErrorString(e_));        \
+            (void)cudaStreamSynchronize(st);                                              \
+            return cf::engine_fail(CF_ECUDA, m_);                                         \
+        }                                                                                 \
+    } while (0)
+
 }  // namespace
 
 extern "C" int cf_mea_scratch(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask,
@@ -178,12 +192,12 @@ extern "C" int cf_mea_scratch(cf_engine* e, const uint8_t* seqs, const int64_t* 
     uint8_t* d_mask = mask ? S + Y.mask : nullptr;
     char* d_structs = reinterpret_cast<char*>(S + Y.structs);
 
-    CF_CUDA_S(cudaMemsetAsync(status, 0, 2 * sizeof(int), st));
-    CF_CUDA_S(cudaMemcpyAsync(d_offs, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
-    if (nbytes) CF_CUDA_S(cudaMemcpyAsync(d_seqs, seqs, nbytes, cudaMemcpyHostToDevice, st));
-    if (mask && nbytes) CF_CUDA_S(cudaMemcpyAsync(d_mask, mask, nbytes, cudaMemcpyHostToDevice, st));
+    CF_CUDA_Q(cudaMemsetAsync(status, 0, 2 * sizeof(int), st));
+    CF_CUDA_Q(cudaMemcpyAsync(d_offs, offsets, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    if (nbytes) CF_CUDA_Q(cudaMemcpyAsync(d_seqs, seqs, nbytes, cudaMemcpyHostToDevice, st));
+    if (mask && nbytes) CF_CUDA_Q(cudaMemcpyAsync(d_mask, mask, nbytes, cudaMemcpyHostToDevice, st));
     k_scratch_descs<<<(n + 255) / 256, 256, 0, st>>>(d_offs, n, d_descs);
-    CF_CUDA_S(cudaGetLastError());
+    CF_CUDA_Q(cudaGetLastError());
 
     cf::WarpArgs W;
     W.descs = d_descs;
@@ -206,13 +220,13 @@ extern "C" int cf_mea_scratch(cf_engine* e, const uint8_t* seqs, const int64_t* 
     W.out = nullptr;
     W.status = status;
     void* args[] = {&W};
-    CF_CUDA_S(cudaLaunchKernel(cf::warp_kernel(mode), dim3((unsigned)grid), dim3(cf::kWarpThreads), args, smem, st));
-    CF_CUDA_S(cudaGetLastError());
+    CF_CUDA_Q(cudaLaunchKernel(cf::warp_kernel(mode), dim3((unsigned)grid), dim3(cf::kWarpThreads), args, smem, st));
+    CF_CUDA_Q(cudaGetLastError());
 
     int h = 0;
-    if (nbytes) CF_CUDA_S(cudaMemcpyAsync(struct_out, d_structs, nbytes, cudaMemcpyDeviceToHost, st));
-    CF_CUDA_S(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CF_CUDA_S(cudaStreamSynchronize(st));
+    if (nbytes) CF_CUDA_Q(cudaMemcpyAsync(struct_out, d_structs, nbytes, cudaMemcpyDeviceToHost, st));
+    CF_CUDA_Q(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CF_CUDA_Q(cudaStreamSynchronize(st));
     if (h != CF_OK) return cf::engine_fail(h, "a kernel reported an internal limit (traceback stack/queue)");
     return CF_OK;
 }

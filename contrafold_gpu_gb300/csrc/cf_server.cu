@@ -436,15 +436,22 @@ int cf_server_replay(cf_server* S, int32_t n, const double* t_arrive, const cf_r
     std::vector<int64_t> tickets(n);
     std::vector<Clock::time_point> due(n);
     const auto t0 = Clock::now();
+    // submit open-loop; a failed submission (e.g. the server is stopping) ends
+    // the submissions, and the requests already in are still collected below
+    int nsub = 0, submit_rc = CF_OK;
+    std::string submit_err;
     for (int k = 0; k < n; ++k) {
         due[k] = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(t_arrive[k]));
         std::this_thread::sleep_until(due[k]);
         const int32_t L = (int32_t)(offsets[k + 1] - offsets[k]);
-        int rc = submit_one(S, &reqs[k], seqs + offsets[k], L, mask ? mask + offsets[k] : nullptr, due[k], &tickets[k]);
-        if (rc) return rc;
+        submit_rc = submit_one(S, &reqs[k], seqs + offsets[k], L, mask ? mask + offsets[k] : nullptr, due[k], &tickets[k]);
+        if (submit_rc) {
+            submit_err = cf_last_error();
+            break;
+        }
+        ++nsub;
     }
-    int first_rc = CF_OK;
-    for (int k = 0; k < n; ++k) {
+    for (int k = 0; k < nsub; ++k) {
         std::unique_lock<std::mutex> lk(S->mu);
         const int64_t tk = tickets[k];
         S->cv_done.wait(lk, [&] {
@@ -454,16 +461,19 @@ int cf_server_replay(cf_server* S, int32_t n, const double* t_arrive, const cf_r
         auto it = S->reqs.find(tk);
         if (it == S->reqs.end()) {   // collected by a wait on the same ticket
             status_out[k] = CF_EINVAL;
+            latency_ms[k] = 0.0;
             continue;
         }
         const int64_t L = offsets[k + 1] - offsets[k];
         const int64_t cap = reqs[k].op == CF_OP_SAMPLE ? L * reqs[k].n_samples : L;
-        const int rc = collect(S, it, reqs[k].op == CF_OP_LOGZ ? logz_out + k : nullptr,
-                               reqs[k].op == CF_OP_LOGZ ? nullptr : out + out_offsets[k], cap, latency_ms + k, due[k]);
-        status_out[k] = rc;
-        if (rc && first_rc == CF_OK) first_rc = rc;
+        status_out[k] = collect(S, it, reqs[k].op == CF_OP_LOGZ ? logz_out + k : nullptr,
+                                reqs[k].op == CF_OP_LOGZ ? nullptr : out + out_offsets[k], cap, latency_ms + k, due[k]);
     }
-    (void)first_rc;
+    for (int k = nsub; k < n; ++k) {   // never submitted
+        status_out[k] = CF_ECANCELLED;
+        latency_ms[k] = 0.0;
+    }
+    if (submit_rc) return fail(submit_rc, "cf_server_replay: submission " + std::to_string(nsub) + " failed: " + submit_err);
     return CF_OK;
 }
 

@@ -176,11 +176,14 @@ int cf_grad(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
  * no constraint) and `d_out` are device pointers laid out like the host
  * buffers of the calls above, and the launches are asynchronous on `stream`
  * (a cudaStream_t; NULL selects the engine's stream).  `d_out` is float[n]
- * for CF_JOB_LOGZ, double[n] for CF_JOB_LOGZ64 and the dot-bracket buffer
- * for CF_JOB_MEA / CF_JOB_MFE.  No reference counterpart: the reference
+ * for CF_JOB_LOGZ, double[n] for CF_JOB_LOGZ64, the dot-bracket buffer
+ * for CF_JOB_MEA / CF_JOB_MFE, and for CF_JOB_BPP the posterior matrices
+ * packed back to back: sequence b's L_b x L_b float32 matrix (as cf_bpp) at
+ * float offset sum_{c<b} L_c^2.  No reference counterpart: the reference
  * re-uploads everything per call (gpu.py:500-514). */
 #define CF_JOB_LOGZ   0
 #define CF_JOB_LOGZ64 1
+#define CF_JOB_BPP    2
 #define CF_JOB_MEA    3
 #define CF_JOB_MFE    4
 typedef struct cf_plan cf_plan;
@@ -264,7 +267,10 @@ int cf_server_cancel(cf_server* server, int64_t ticket);
  * when all are done.  Sequences and masks are laid out as in cf_logz; outputs
  * go to logz_out[k] (logZ) or out[out_offsets[k] ..] (MEA: L bytes, samples:
  * n_samples * L bytes); latency_ms[k] = completion - scheduled arrival;
- * status_out[k] = the request's status. */
+ * status_out[k] = the request's status.  If a submission fails (e.g. the
+ * server is stopping), the requests already submitted are still collected,
+ * the rest get status CF_ECANCELLED, and the call returns the submission's
+ * error. */
 int cf_server_replay(cf_server* server, int32_t n, const double* t_arrive,
                      const cf_request* reqs, const uint8_t* seqs, const int64_t* offsets,
                      const uint8_t* mask, const int64_t* out_offsets, float* logz_out,

@@ -575,242 +575,44 @@ size_t oracle_posterior32_tabs_len(int L) {
     return 7 * n * n + 2 * n;
 }
 
-/* posterior (cpu.py:583-820).  POST (L+2)x(L+2) row-major, 1-based, clipped.
- * Returns Z = F5[L] (FP32). */
-float oracle_posterior32(const int8_t* s, int L, const int8_t* forced, const float* blob,
-                         float* POST, float* tabs) {
-    P32 P = unpack32(blob);
-    const int n = L + 2;
-    const size_t nn = (size_t)n * n;
-    float* buf = (float*)malloc(sizeof(float) * (6 * nn + 2 * n));
-    float *FC = buf, *FM = buf + nn, *FM1 = buf + 2 * nn;
-    float *FCo = buf + 3 * nn, *FMo = buf + 4 * nn, *FM1o = buf + 5 * nn;
-    float *F5 = buf + 6 * nn, *F5o = F5 + n;
-    for (size_t t = 0; t < 6 * nn + 2 * n; ++t) buf[t] = NEG32;
-    const float ZERO = F(0.0);
+/* posterior (cpu.py:583-820), float32: the body is cf_oracle_post.inc */
+#define PR float
+#define PF_NAME oracle_posterior32
+#define PF_PARAMS P32
+#define PF_UNPACK unpack32
+#define PF_NEG NEG32
+#define PF_HALF HALF32
+#define PF_LSE lse32
+#define PF_EXP fexp32
+#include "cf_oracle_post.inc"
+#undef PR
+#undef PF_NAME
+#undef PF_PARAMS
+#undef PF_UNPACK
+#undef PF_NEG
+#undef PF_HALF
+#undef PF_LSE
+#undef PF_EXP
 
-    for (int i = L; i >= 0; --i) {
-        for (int j = i; j <= L; ++j) {
-            float FM2 = NEG32;
-            for (int k = i + 1; k < j; ++k)
-                if (T(FM1, i, k) > HALF32 && T(FM, k, j) > HALF32)
-                    { CNT(1); FM2 = lse32(FM2, T(FM1, i, k) + T(FM, k, j)); }
-            if (0 < i && j < L && OK_PAIR(i, j + 1)) {
-                float sum = NEG32;
-                float jB = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                CNT(2); sum = lse32(sum, jB + P.hp[j - i <= DHP ? j - i : DHP]);
-                int pmax = i + CMAX < j ? i + CMAX : j;
-                for (int p = i; p <= pmax; ++p) {
-                    int l1 = p - i;
-                    int qmin = p + 2, alt = p - i + j - CMAX;
-                    if (alt > qmin) qmin = alt;
-                    for (int q = j; q >= qmin; --q) {
-                        int l2 = j - q;
-                        if (OK_PAIR(p + 1, q) && T(FC, p + 1, q - 1) > HALF32) {
-                            float e;
-                            if (p == i && q == j) {
-                                e = P.bp[I2(s[i + 1], s[j])] + P.stack[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                            } else {
-                                float jB1 = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                                float jB2 = P.hc[I2(s[q], s[p + 1])] + P.tm[I4(s[q], s[p + 1], s[q + 1], s[p])];
-                                float snuc = ZERO;
-                                if (l1 == 0 && l2 == 1) snuc = P.b01[s[j]];
-                                else if (l1 == 1 && l2 == 0) snuc = P.b01[s[i + 1]];
-                                else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
-                                e = P.cs[l1 * 31 + l2] + P.bp[I2(s[p + 1], s[q])] + jB1 + jB2 + snuc;
-                            }
-                            CNT(0); sum = lse32(sum, e + T(FC, p + 1, q - 1));
-                        }
-                    }
-                }
-                if (FM2 > HALF32) {
-                    float jA = P.hc[I2(s[i], s[j + 1])];
-                    if (i < L) jA += P.dl[I3(s[i], s[j + 1], s[i + 1])];
-                    if (j > 0) jA += P.dr[I3(s[i], s[j + 1], s[j])];
-                    CNT(2); sum = lse32(sum, FM2 + jA + P.mp + P.mb);
-                }
-                T(FC, i, j) = sum;
-            }
-            if (0 < i && i + 2 <= j && j < L) {
-                float sum = NEG32;
-                if (OK_PAIR(i + 1, j) && T(FC, i + 1, j - 1) > HALF32) {
-                    float jAji = P.hc[I2(s[j], s[i + 1])];
-                    if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
-                    if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    CNT(2); sum = lse32(sum, T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
-                }
-                if (T(FM1, i + 1, j) > HALF32) { CNT(2); sum = lse32(sum, T(FM1, i + 1, j) + P.mu); }
-                T(FM1, i, j) = sum;
-            }
-            if (0 < i && i + 2 <= j && j < L) {
-                float sum = NEG32;
-                if (FM2 > HALF32) { CNT(2); sum = lse32(sum, FM2); }
-                if (T(FM, i, j - 1) > HALF32) { CNT(2); sum = lse32(sum, T(FM, i, j - 1) + P.mu); }
-                if (T(FM1, i, j) > HALF32) { CNT(2); sum = lse32(sum, T(FM1, i, j)); }
-                T(FM, i, j) = sum;
-            }
-        }
-    }
-    F5[0] = ZERO;
-    for (int j = 1; j <= L; ++j) {
-        float sum = F5[j - 1] + P.eu;
-        for (int k = 0; k < j; ++k) {
-            if (OK_PAIR(k + 1, j) && T(FC, k + 1, j - 1) > HALF32 && F5[k] > HALF32) {
-                float jA = P.hc[I2(s[j], s[k + 1])];
-                if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
-                if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
-                CNT(2); sum = lse32(sum, F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
-            }
-        }
-        F5[j] = sum;
-    }
-    const float Z = F5[L];
-
-    /* ---------- outside (cpu.py:680-758) ---------- */
-    F5o[L] = ZERO;
-    for (int j = L; j > 0; --j) {
-        CNT(5); F5o[j - 1] = lse32(F5o[j - 1], F5o[j] + P.eu);
-        for (int k = 0; k < j; ++k) {
-            if (OK_PAIR(k + 1, j)) {
-                float jA = P.hc[I2(s[j], s[k + 1])];
-                if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
-                if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
-                float temp = F5o[j] + P.ep + P.bp[I2(s[k + 1], s[j])] + jA;
-                if (T(FC, k + 1, j - 1) > HALF32) { CNT(5); F5o[k] = lse32(F5o[k], temp + T(FC, k + 1, j - 1)); }
-                if (F5[k] > HALF32) { CNT(5); T(FCo, k + 1, j - 1) = lse32(T(FCo, k + 1, j - 1), temp + F5[k]); }
-            }
-        }
-    }
-    for (int i = 0; i <= L; ++i) {
-        for (int j = L; j >= i; --j) {
-            float FM2o = NEG32;
-            if (0 < i && i + 2 <= j && j < L) {
-                CNT(5); CNT(5); CNT(5); FM2o = lse32(FM2o, T(FMo, i, j));
-                T(FMo, i, j - 1) = lse32(T(FMo, i, j - 1), T(FMo, i, j) + P.mu);
-                T(FM1o, i, j) = lse32(T(FM1o, i, j), T(FMo, i, j));
-            }
-            if (0 < i && i + 2 <= j && j < L) {
-                if (OK_PAIR(i + 1, j)) {
-                    float jAji = P.hc[I2(s[j], s[i + 1])];
-                    if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
-                    if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    CNT(5); T(FCo, i + 1, j - 1) = lse32(T(FCo, i + 1, j - 1), T(FM1o, i, j) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])]);
-                }
-                CNT(5); T(FM1o, i + 1, j) = lse32(T(FM1o, i + 1, j), T(FM1o, i, j) + P.mu);
-            }
-            if (0 < i && j < L && OK_PAIR(i, j + 1)) {
-                float fco = T(FCo, i, j);
-                if (fco > HALF32) {
-                    float jB_ij = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                    int pmax = i + CMAX < j ? i + CMAX : j;
-                    for (int p = i; p <= pmax; ++p) {
-                        int l1 = p - i;
-                        int qmin = p + 2, alt = p - i + j - CMAX;
-                        if (alt > qmin) qmin = alt;
-                        for (int q = j; q >= qmin; --q) {
-                            int l2 = j - q;
-                            if (OK_PAIR(p + 1, q)) {
-                                float e;
-                                if (p == i && q == j) {
-                                    e = P.bp[I2(s[i + 1], s[j])] + P.stack[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                                } else {
-                                    float jB2 = P.hc[I2(s[q], s[p + 1])] + P.tm[I4(s[q], s[p + 1], s[q + 1], s[p])];
-                                    float snuc = ZERO;
-                                    if (l1 == 0 && l2 == 1) snuc = P.b01[s[j]];
-                                    else if (l1 == 1 && l2 == 0) snuc = P.b01[s[i + 1]];
-                                    else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
-                                    e = P.cs[l1 * 31 + l2] + P.bp[I2(s[p + 1], s[q])] + jB_ij + jB2 + snuc;
-                                }
-                                CNT(3); T(FCo, p + 1, q - 1) = lse32(T(FCo, p + 1, q - 1), fco + e);
-                            }
-                        }
-                    }
-                    float jA = P.hc[I2(s[i], s[j + 1])];
-                    if (i < L) jA += P.dl[I3(s[i], s[j + 1], s[i + 1])];
-                    if (j > 0) jA += P.dr[I3(s[i], s[j + 1], s[j])];
-                    CNT(5); FM2o = lse32(FM2o, fco + jA + P.mp + P.mb);
-                }
-            }
-            if (FM2o > HALF32) {
-                for (int k = i + 1; k < j; ++k) {
-                    if (T(FM, k, j) > HALF32) { CNT(4); T(FM1o, i, k) = lse32(T(FM1o, i, k), FM2o + T(FM, k, j)); }
-                    if (T(FM1, i, k) > HALF32) { CNT(4); T(FMo, k, j) = lse32(T(FMo, k, j), FM2o + T(FM1, i, k)); }
-                }
-            }
-        }
-    }
-
-    /* ---------- posterior (cpu.py:760-819) ---------- */
-    for (size_t t = 0; t < nn; ++t) POST[t] = ZERO;
-    for (int i = L; i >= 0; --i) {
-        for (int j = i; j <= L; ++j) {
-            if (0 < i && j < L && OK_PAIR(i, j + 1)) {
-                float outside = T(FCo, i, j) - Z;
-                if (outside > HALF32) {
-                    float jB_ij = P.hc[I2(s[i], s[j + 1])] + P.tm[I4(s[i], s[j + 1], s[i + 1], s[j])];
-                    int pmax = i + CMAX < j ? i + CMAX : j;
-                    for (int p = i; p <= pmax; ++p) {
-                        int l1 = p - i;
-                        int qmin = p + 2, alt = p - i + j - CMAX;
-                        if (alt > qmin) qmin = alt;
-                        for (int q = j; q >= qmin; --q) {
-                            int l2 = j - q;
-                            if (OK_PAIR(p + 1, q) && T(FC, p + 1, q - 1) > HALF32) {
-                                float e;
-                                if (p == i && q == j) {
-                                    e = outside + P.bp[I2(s[i + 1], s[j])] + P.stack[I4(s[i], s[j + 1], s[i + 1], s[j])] + T(FC, p + 1, q - 1);
-                                } else {
-                                    float jB2 = P.hc[I2(s[q], s[p + 1])] + P.tm[I4(s[q], s[p + 1], s[q + 1], s[p])];
-                                    float snuc = ZERO;
-                                    if (l1 == 0 && l2 == 1) snuc = P.b01[s[j]];
-                                    else if (l1 == 1 && l2 == 0) snuc = P.b01[s[i + 1]];
-                                    else if (l1 == 1 && l2 == 1) snuc = P.i11[I2(s[i + 1], s[j])];
-                                    e = outside + jB_ij + P.cs[l1 * 31 + l2] + T(FC, p + 1, q - 1) + P.bp[I2(s[p + 1], s[q])] + jB2 + snuc;
-                                }
-                                CNT(6); T(POST, p + 1, q) += fexp32(e);
-                            }
-                        }
-                    }
-                }
-            }
-            if (0 < i && i + 2 <= j && j < L) {
-                if (OK_PAIR(i + 1, j) && T(FC, i + 1, j - 1) > HALF32 && T(FM1o, i, j) > HALF32) {
-                    float jAji = P.hc[I2(s[j], s[i + 1])];
-                    if (j < L) jAji += P.dl[I3(s[j], s[i + 1], s[j + 1])];
-                    if (i > 0) jAji += P.dr[I3(s[j], s[i + 1], s[i])];
-                    CNT(6); T(POST, i + 1, j) += fexp32(T(FM1o, i, j) + T(FC, i + 1, j - 1) + jAji + P.mp + P.bp[I2(s[i + 1], s[j])] - Z);
-                }
-            }
-        }
-    }
-    for (int j = 1; j <= L; ++j) {
-        float outside = F5o[j] - Z;
-        if (outside > HALF32) {
-            for (int k = 0; k < j; ++k) {
-                if (OK_PAIR(k + 1, j) && T(FC, k + 1, j - 1) > HALF32 && F5[k] > HALF32) {
-                    float jA = P.hc[I2(s[j], s[k + 1])];
-                    if (j < L) jA += P.dl[I3(s[j], s[k + 1], s[j + 1])];
-                    if (k > 0) jA += P.dr[I3(s[j], s[k + 1], s[k])];
-                    CNT(6); T(POST, k + 1, j) += fexp32(outside + F5[k] + T(FC, k + 1, j - 1) + P.ep + P.bp[I2(s[k + 1], s[j])] + jA);
-                }
-            }
-        }
-    }
-    for (int i = 1; i <= L; ++i)
-        for (int j = i + 1; j <= L; ++j) {
-            float v = T(POST, i, j);
-            if (v < ZERO) v = ZERO;
-            else if (v > F(1.0)) v = F(1.0);
-            T(POST, i, j) = v;
-        }
-    if (tabs) {
-        memcpy(tabs, buf, sizeof(float) * 6 * nn);
-        memcpy(tabs + 6 * nn, POST, sizeof(float) * nn);
-        memcpy(tabs + 7 * nn, F5, sizeof(float) * 2 * n);
-    }
-    free(buf);
-    return Z;
-}
+/* The same recurrences in float64 with exact log-sum-exp and exp: the exact
+ * pair probabilities (ours; test oracle of the sampler's frequencies). */
+#define PR double
+#define PF_NAME oracle_posterior64x
+#define PF_PARAMS P64
+#define PF_UNPACK unpack64
+#define PF_NEG NEG64
+#define PF_HALF HALF64
+#define PF_LSE lse64
+#define PF_EXP exp
+#include "cf_oracle_post.inc"
+#undef PR
+#undef PF_NAME
+#undef PF_PARAMS
+#undef PF_UNPACK
+#undef PF_NEG
+#undef PF_HALF
+#undef PF_LSE
+#undef PF_EXP
 
 /* MEA decode (cpu.py:823-895).  POST is (L+2)x(L+2) as from oracle_posterior32. */
 void oracle_mea_decode32(const float* POST, int L, const int8_t* forced, const int8_t* s,

@@ -10,6 +10,7 @@ Functions mirror the reference's host wrappers:
   bpp(seq, P, forced)      -> cpu.bpp                   (cpu.py:926-929)
   mea(seq, P, gamma, forced) -> cpu.mea                 (cpu.py:932-941)
   mfe(seq, P, forced)      -> cpu.mfe                   (cpu.py:505-519)
+  bpp_exact(seq, P, forced) -> the same posterior in FP64 with exact log1p/exp (ours)
 """
 from __future__ import annotations
 
@@ -28,8 +29,8 @@ JOB_MEA, JOB_MFE, JOB_LOGZ64, JOB_LOGZ32 = 0, 1, 2, 3
 
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the recipe in oracle/Makefile."""
-    src = os.path.join(HERE, "cf_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("cf_oracle.c", "cf_oracle_post.inc", "Makefile")]
+    if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(LIB_PATH) < os.path.getmtime(f) for f in srcs):
         subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
     return LIB_PATH
 
@@ -47,6 +48,8 @@ def lib():
         L.oracle_viterbi64.argtypes = [i8p, ctypes.c_int, i8p, f64p, i64p]
         L.oracle_posterior32.restype = ctypes.c_float
         L.oracle_posterior32.argtypes = [i8p, ctypes.c_int, i8p, f32p, f32p, f32p]
+        L.oracle_posterior64x.restype = ctypes.c_double
+        L.oracle_posterior64x.argtypes = [i8p, ctypes.c_int, i8p, f64p, f64p, f64p]
         L.oracle_posterior32_tabs_len.restype = ctypes.c_size_t
         L.oracle_posterior32_tabs_len.argtypes = [ctypes.c_int]
         L.oracle_mea_decode32.restype = None
@@ -154,6 +157,20 @@ def bpp(seq, P, forced=None) -> np.ndarray:
     return POST[1:L + 1, 1:L + 1].astype(np.float64)
 
 
+def bpp_exact(seq, P, forced=None) -> np.ndarray:
+    """Exact Boltzmann pair probabilities: the posterior recurrences of
+    cpu.py:583-820 in float64 with exact log1p/exp (ours; the reference's
+    posterior is the float32 Fast_LogPlusEquals / Fast_Exp one, 1-6 % off the
+    exact probabilities).  The sampler draws from this distribution."""
+    s, fo, L = encode(seq, forced)
+    _, b64 = _blobs(P)
+    n = L + 2
+    POST = np.empty((n, n), np.float64)
+    lib().oracle_posterior64x(_ptr(s, ctypes.c_int8), L, _ptr(fo, ctypes.c_int8), _ptr(b64, ctypes.c_double),
+                              _ptr(POST, ctypes.c_double), None)
+    return POST[1:L + 1, 1:L + 1].copy()
+
+
 def _db(pair, L):
     ch = ["."] * L
     for t in range(1, L + 1):
@@ -219,11 +236,15 @@ def batch(job, seqs, P, masks=None, gamma=6.0, threads=None):
 
 
 # Cost, in FP32 operations, of one guarded update of each counter category
-# (oracle_count_mea_ops): single-branch LSE = 5 adds for the loop score +
-# 1 add of the inner value + 8 for Fast_LogPlusEquals; bifurcation / other
-# LSE = 1 add + 8; posterior term = 7 adds + 8 (Fast_Exp) + 1 accumulate;
-# MEA candidate = 1 add (the compare is not counted).
-OP_COST = (14, 9, 9, 14, 9, 9, 16, 1)
+# (oracle_count_mea_ops), the cost model of the fold's roofline: single-branch
+# LSE = 4 adds for the loop score + 1 for jB2 + 1 add of the inner value + 8 for
+# Fast_LogPlusEquals (sub, 3 mul, 3 add, final add) = 14; bifurcation / other
+# LSE = 1 add + 8 = 9; posterior Fast_Exp term = 8; MEA max-plus candidate = 1.
+OP_COST = (14, 9, 9, 14, 9, 9, 8, 1)
+# FP64 operations of the Viterbi forward pass per inside category (the same
+# guarded candidates as the inside): single-branch = 5 adds + 1 compare,
+# bifurcation = 1 add + 1 compare, other terms = 3 adds + 1 compare.
+VITERBI_COST = (6, 2, 4)
 COUNT_NAMES = ("inside_single", "inside_bif", "inside_other", "outside_single", "outside_bif",
                "outside_other", "posterior_terms", "mea_candidates")
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference engine itself.
 
 Imports the reference's CPU engine (gpu_contrafold/cpu.py, read from the
-reference checkout given by --ref, default /root/reference) under an identity
+reference checkout given by the required --ref argument) under an identity
 `numba.njit` stub -- numba is not installed here, so the reference runs as
 plain Python/numpy with the same float32/float64 scalar semantics -- and
 records, for seeded inputs:
@@ -16,22 +16,22 @@ records, for seeded inputs:
     and the sequences of its validation script (tests/test_validation.py:15-27).
 
 Run once in a container that has the reference checkout:
-    python tests/golden/make_golden.py [--ref /root/reference] [--jobs 8]
+    python tests/golden/make_golden.py --ref <reference checkout> [--jobs 8]
 The output, tests/golden/golden.json (+ params_blob64.npy), is committed; the
 tests read only those files.
 
-    python tests/golden/make_golden.py --exhaustive
+    python tests/golden/make_golden.py --ref <reference checkout> --exhaustive
 writes tests/golden/exhaustive.json.gz instead: every ACGU sequence of 1-5 nt
 without a mask and every (sequence, mask) pair of 1-4 nt, each with FP64 logZ,
 the Viterbi and MEA (gamma 6) structures and the first 16 hex digits of the
 SHA-256 of its float32 posterior matrix.
 
-    python tests/golden/make_golden.py --long
+    python tests/golden/make_golden.py --ref <reference checkout> --long
 writes tests/golden/long.json: seven seeded sequences of 300-600 nt (masks
 Bernoulli 0.1 / 0.3 on some, N on one) with the same fields as golden.json
 (minutes per case: the reference runs as plain Python).
 
-    python tests/golden/make_golden.py --xlong
+    python tests/golden/make_golden.py --ref <reference checkout> --xlong
 writes tests/golden/xlong.json: one 800-nt and one 1,000-nt sequence (the
 latter with a Bernoulli 0.1 mask), about an hour of pure Python.
 """
@@ -222,7 +222,7 @@ def validation_script_sequences():
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="checkout of the reference (the directory holding gpu_contrafold/)")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--out", default=None)
     ap.add_argument("--exhaustive", action="store_true", help="all short sequences (and masks): exhaustive.json.gz")

@@ -1,8 +1,10 @@
 """Sampler checks: structure validity, forced-unpaired masks, reproducibility and
-pair frequencies against the posterior within 3 sigma binomial noise
-(the reference's own checks 3 and 4, tests/test_validation.py:44-76)."""
+pair frequencies against the exact pair probabilities within 3 sigma binomial
+noise (the reference's own checks 3 and 4, tests/test_validation.py:44-76)."""
 import numpy as np
 import pytest
+
+from conftest import check_pair_frequencies
 
 pytestmark = pytest.mark.gpu
 
@@ -65,18 +67,11 @@ def test_sample_forced_unpaired_mask(engine, golden):
 
 @pytest.mark.parametrize("seq,n", [("GCGCGCAAAAGCGCGCAAAAGCGC", 20000)])
 def test_sample_frequencies_match_posterior(engine, P, oracle, seq, n):
-    """Pair frequencies vs posteriors: |f - p| <= 3 sqrt(p(1-p)/N) + 1/N for every pair."""
+    """Pair frequencies vs the exact pair probabilities (the distribution the
+    sampler draws from): per pair within 3 sigma + 1/N (conftest.check_pair_frequencies)."""
     from contrafold_gpu_gb300.engine import Batch
-    L = len(seq)
     out = engine.sample(Batch([seq]), n, seed=1)[0]
-    f = np.zeros((L, L))
-    for db in out:
-        for x, y in _pairs(db):
-            f[x, y] += 1
-    f /= n
-    p = oracle.bpp(seq, P)
-    tol = 3 * np.sqrt(p * (1 - p) / n) + 1.0 / n
-    assert np.all(np.abs(f - p) <= tol + 2e-4), np.max(np.abs(f - p) - tol)
+    check_pair_frequencies(out, oracle.bpp_exact(seq, P), n)
 
 
 def test_sample_frequencies_random_masked(engine, P, oracle):
@@ -86,14 +81,7 @@ def test_sample_frequencies_random_masked(engine, P, oracle):
     seq = "".join(rng.choice(list("ACGU"), size=L))
     mask = (rng.random(L) < 0.1).astype(np.int8)
     out = engine.sample(Batch([seq], [mask]), n, seed=5)[0]
-    f = np.zeros((L, L))
-    for db in out:
-        for x, y in _pairs(db):
-            f[x, y] += 1
-    f /= n
-    p = oracle.bpp(seq, P, mask)
-    tol = 3.5 * np.sqrt(p * (1 - p) / n) + 1.0 / n
-    assert np.all(np.abs(f - p) <= tol + 2e-4), np.max(np.abs(f - p) - tol)
+    check_pair_frequencies(out, oracle.bpp_exact(seq, P, mask), n)
 
 
 def test_fold_tasks_gpu_api(P):

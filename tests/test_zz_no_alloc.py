@@ -62,6 +62,50 @@ def test_scratch_matches_cf_mea_on_consecutive_calls(engine):
     assert free1 == free0, "device memory changed across calls that should allocate nothing"
 
 
+def _pad32(w):
+    return (w + 31) & ~31
+
+
+def _slot_bytes(L):
+    """Bytes of one warp fold slot for a longest sequence of L nt: the float32
+    fold arena of the kernels (csrc/cf_device.cuh arena32): seven triangular
+    tables, five (L + 2)-vectors, the pair list and the traceback queue."""
+    t = _pad32((L + 1) * (L + 2) // 2)
+    v = _pad32(L + 2)
+    plist = _pad32(L + 3) + _pad32((L + 1) * (L + 2) // 4 + 1)   # int32 offsets + int16 list
+    return 4 * (7 * t + 5 * v + plist + _pad32(4 * L + 16))
+
+
+def _scratch_limit(nbytes, n=1):
+    """Longest sequence for which a batch of n sequences, nbytes nucleotides and
+    no mask leaves room for one CTA (8 warps) of fold slots in the scratch
+    (csrc/cf_noalloc.cu layout_for)."""
+    up = lambda x: (x + 255) & ~255
+    arena = 256 + up(8 * (n + 1)) + up(24 * n) + up(nbytes) + up(nbytes)
+    L = 1
+    while 8 * _slot_bytes(L + 1) <= SCRATCH_BYTES - arena:
+        L += 1
+    return L
+
+
+@pytest.mark.gpu
+def test_scratch_at_the_length_limit(engine):
+    """One sequence just at the longest length whose 8 fold slots fit folds like
+    cf_mea; one nucleotide more is rejected with CF_EINVAL."""
+    lim = _scratch_limit(0)
+    lim = _scratch_limit(lim)          # the sequence's own input and output bytes
+    assert 700 <= lim <= 800, lim
+    rng = np.random.default_rng(31)
+    seq = "".join(rng.choice(list("ACGU"), size=lim))
+    B = Batch([seq])
+    assert _mea_scratch(engine, B) == engine.mea(B)
+    lib, f = _scratch_fn()
+    B1 = Batch([seq + "A"])
+    out = ctypes.create_string_buffer(B1.total)
+    rc = f(engine._h, _p(B1.buf, ctypes.c_uint8), _p(B1.offsets, ctypes.c_int64), None, 1, 6.0, out)
+    assert rc == CF_EINVAL and b"scratch" in lib.cf_last_error()
+
+
 @pytest.mark.gpu
 def test_scratch_rejects_what_does_not_fit(engine):
     lib, f = _scratch_fn()
