@@ -5,17 +5,29 @@ forced-unpaired mask) on the GPU under every schedule the engine offers --
 the persistent warp-per-sequence kernel and the persistent CTA-per-sequence
 fused kernel at 1..4 resident CTAs per SM -- and reports folds/s per choice
 and the best one per bucket.  Every schedule computes identical results; only
-speed differs.  The engine's built-in length table (cf_engine.cu,
-auto_warp_max_len / auto_ctas_per_sm) is set from these measurements.
+speed differs.  The engine's built-in schedule table (cf_engine.cu,
+default_tuning) was set from these measurements.
 
     python -m contrafold_gpu_gb300.autotune [--lengths 50,100,200,300,400] [--json out.json]
     python -m contrafold_gpu_gb300.autotune --lengths 100,200 --batch-sizes 256,1024,4096
     python -m contrafold_gpu_gb300.autotune --latency --lengths 150,400,600,1000 --batch-sizes 1,16,32
 
 --latency times small batches of long sequences (ms per batch) on the grouped
-and the cluster schedules -- the engine's auto_cluster_min_len -- and, with
---phase-timing, the grouped schedule's per-phase kernels; --mask-frac sets the
-forced-unpaired fraction (1.0: no pairable cell, the bifurcation chains alone).
+and the cluster schedules and, with --phase-timing, the grouped schedule's
+per-phase kernels; --mask-frac sets the forced-unpaired fraction (1.0: no
+pairable cell, the bifurcation chains alone).
+
+--write-table FILE runs the sweeps that decide the automatic schedule and
+writes the engine's schedule table (include/contrafold_gb300.h,
+cf_engine_load_tuning): for mixed-length batches (lengths uniform in
+[Lmax/2, Lmax]) of each --lengths x --batch-sizes cell, the faster of the
+warp and grouped schedules (MEA folds/s); for small batches of long
+sequences, the grouped or the cluster schedule (ms per batch).  The engine
+reads the table through Engine.load_tuning(FILE) or, at creation, from the
+environment variable CONTRAFOLD_GB300_TUNING.
+
+    python -m contrafold_gpu_gb300.autotune --write-table tuning.txt \
+        --lengths 80,160,256 --batch-sizes 512,2048,8192 --long-lengths 512,768 --long-batches 8,38
 """
 from __future__ import annotations
 
@@ -92,6 +104,61 @@ def time_schedule(P, L, n, kind, ctas, reps=3, job="mea", group=0):
     return n / (best / 1000.0)
 
 
+def _mixed_batch(n, Lmax, seed):
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(max(1, Lmax // 2), Lmax + 1, n)
+    lens[0] = Lmax
+    seqs = [np.frombuffer(b"ACGU", np.uint8)[rng.integers(0, 4, int(L))].tobytes().decode() for L in lens]
+    masks = [(rng.random(int(L)) < 0.1).astype(np.int8) for L in lens]
+    return seqs, masks
+
+
+def time_mixed(P, n, Lmax, kind, reps=2):
+    """MEA folds/s of a mixed-length batch on schedule `kind` (host buffers, best of reps)."""
+    from .engine import Batch, Engine
+    seqs, masks = _mixed_batch(n, Lmax, 11)
+    B = Batch(seqs, masks)
+    eng = Engine(P)
+    eng.set_schedule(kind)
+    eng.mea(B, 6.0)
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        eng.mea(B, 6.0)
+        best = min(best, time.perf_counter() - t0)
+    eng.close()
+    return n / best
+
+
+def tuning_rows(P, lengths, batch_sizes, long_lengths, long_batches, log=print):
+    """Measure and return the schedule table as text rows (first match wins)."""
+    rows = ["# contrafold-gb300 schedule table, written by contrafold_gpu_gb300.autotune --write-table",
+            "# min_len max_len min_batch max_batch uniform jobs schedule group ctas_per_sm"]
+    # long sequences, small batches: cluster vs grouped latency (longer minimum
+    # lengths first: the first matching row wins)
+    for Lo in sorted(long_lengths, reverse=True):
+        for n in sorted(long_batches):
+            g_ms, _ = time_latency(P, Lo, n, "group")
+            c_ms, _ = time_latency(P, Lo, n, "cluster")
+            best = "cluster" if c_ms < g_ms else "group"
+            log(f"long L>={Lo} n<={n}: group {g_ms:.1f} ms cluster {c_ms:.1f} ms -> {best}")
+            rows.append(f"{Lo} 32767 1 {n} any logz,bpp,mea,sample {best} 0 0")
+    # mixed lengths: warp vs grouped throughput, most specific rows first
+    prev = 0
+    for Lmax in sorted(lengths):
+        cells = []
+        for n in sorted(batch_sizes):
+            w = time_mixed(P, n, Lmax, "warp")
+            g = time_mixed(P, n, Lmax, "group")
+            best = "warp" if w > g else "group"
+            log(f"mixed {prev + 1}-{Lmax} nt n={n}: warp {w:.0f} group {g:.0f} folds/s -> {best}")
+            cells.append((n, best))
+        for n, best in sorted(cells, reverse=True):
+            rows.append(f"0 {Lmax} {n} 0 mixed logz,bpp,mea {best} 0 0")
+        prev = Lmax
+    return rows
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--lengths", default="50,100,200,300,400")
@@ -108,9 +175,22 @@ def main():
                     help="ms per small batch on the grouped and cluster schedules (lengths x --batch-sizes)")
     ap.add_argument("--mask-frac", type=float, default=0.1, help="--latency: forced-unpaired fraction")
     ap.add_argument("--phase-timing", action="store_true", help="--latency: grouped per-phase kernel times")
+    ap.add_argument("--write-table", default=None, metavar="FILE",
+                    help="measure and write the engine's schedule table (--lengths, --batch-sizes, --long-lengths, "
+                         "--long-batches)")
+    ap.add_argument("--long-lengths", default="512,768")
+    ap.add_argument("--long-batches", default="8,38")
     args = ap.parse_args()
     from . import load
     P = load()
+    if args.write_table:
+        ints = lambda x: [int(v) for v in x.split(",")]
+        rows = tuning_rows(P, ints(args.lengths), ints(args.batch_sizes or "512,2048,8192"),
+                           ints(args.long_lengths), ints(args.long_batches))
+        with open(args.write_table, "w") as fh:
+            fh.write("\n".join(rows) + "\n")
+        print(f"wrote {len(rows) - 2} rows -> {args.write_table}")
+        return rows
     if args.latency:
         table = {}
         for L in [int(x) for x in args.lengths.split(",")]:

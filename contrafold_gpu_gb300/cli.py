@@ -9,8 +9,8 @@
     gpu-contrafold seqs.fa --parens out.parens   # structures also as a CONTRAfold parens file
     gpu-contrafold seqs.fa --posteriors 1e-5 out.post   # sparse posterior file (CONTRAfold format)
 
-Same arguments, input sniffing, mask validation, mode precedence and output
-format as the reference (cli.py:88-230).  The difference is where the work
+Same arguments, input behaviour (below), mode precedence and output format
+as the reference (cli.py:88-230).  The difference is where the work
 runs: MEA and Viterbi structures are folded in length-sorted batches on the
 GPU (the reference folds them one record at a time on the CPU,
 cli.py:188-193), and every mode goes through the same engine.
@@ -37,90 +37,108 @@ import argparse
 import json
 import os
 import sys
+from typing import Any, Iterable, List, NamedTuple, Tuple
 
 import numpy as np
 
-_SEQ_CHARS = set("ACGUTN")
+# Input behaviour (kept for drop-in use; the reference's CLI accepts the same):
+#  * the argument names an existing file, or else is itself one sequence of the
+#    letters A C G U T N in any case (anything else is an error exit);
+#  * a file's format is decided by the first character of its first non-blank
+#    line: "{" JSON lines, ">" FASTA, anything else one sequence per line;
+#  * JSON lines: one object per non-blank line with "seq" (required, non-empty)
+#    and optional "id" (default: the 0-based line number) and "constrain";
+#    malformed JSON or a missing "seq" is an error exit naming the line;
+#  * FASTA: a ">" line opens a record named by the rest of the line (or, when
+#    that is empty, by how many records precede it); its sequence is the
+#    following non-blank lines joined; a record without sequence is dropped;
+#  * sequence per line: every non-blank line is a record named by its 0-based
+#    line number;
+#  * sequences are upper-cased and stripped of surrounding white space;
+#  * "constrain" is a 0/1 list or a string in which "1" marks a forced-unpaired
+#    position (any other character is 0); it must have one entry per base and
+#    list entries must be 0 or 1 -- otherwise an error exit.
+_NUCLEOTIDES = frozenset("ACGUTN")
 
 
-def _parse_jsonl(path):
-    recs = []
-    with open(path) as fh:
-        for ln, line in enumerate(fh):
-            line = line.strip()
-            if not line:
-                continue
-            try:
-                obj = json.loads(line)
-            except json.JSONDecodeError as e:
-                raise SystemExit(f"line {ln}: invalid JSON ({e})")
-            if "seq" not in obj or not obj["seq"]:
-                raise SystemExit(f"line {ln}: missing required field 'seq'")
-            recs.append((obj.get("id", ln), str(obj["seq"]).strip().upper(), obj.get("constrain")))
-    return recs
+class Record(NamedTuple):
+    id: Any
+    seq: str
+    constrain: Any = None
 
 
-def _parse_fasta(path):
-    recs, rid, cur = [], None, []
-    with open(path) as fh:
-        for line in fh:
-            line = line.rstrip("\n")
-            if line.startswith(">"):
-                if cur:
-                    recs.append((rid, "".join(cur).upper(), None))
-                    cur = []
-                rid = line[1:].strip() or len(recs)
-            elif line.strip():
-                cur.append(line.strip())
-    if cur:
-        recs.append((rid, "".join(cur).upper(), None))
-    return recs
+def _read_jsonl(numbered: Iterable[Tuple[int, str]]) -> List[Record]:
+    out: List[Record] = []
+    for lineno, text in numbered:
+        if not text.strip():
+            continue
+        try:
+            obj = json.loads(text)
+        except json.JSONDecodeError as err:
+            raise SystemExit(f"line {lineno}: invalid JSON ({err})")
+        seq = obj.get("seq") if isinstance(obj, dict) else None
+        if not seq:
+            raise SystemExit(f"line {lineno}: missing required field 'seq'")
+        out.append(Record(obj.get("id", lineno), str(seq).strip().upper(), obj.get("constrain")))
+    return out
 
 
-def _parse_seq_lines(path):
-    recs = []
-    with open(path) as fh:
-        for i, line in enumerate(fh):
-            s = line.strip().upper()
-            if s:
-                recs.append((i, s, None))
-    return recs
+def _read_fasta(numbered: Iterable[Tuple[int, str]]) -> List[Record]:
+    out: List[Record] = []
+    name: Any = None
+    parts: List[str] = []
+
+    def close():
+        if parts:
+            out.append(Record(name, "".join(parts).upper()))
+
+    for _, text in numbered:
+        if text.startswith(">"):
+            close()
+            parts = []
+            name = text[1:].strip() or len(out)
+        elif text.strip():
+            parts.append(text.strip())
+    close()
+    return out
 
 
-def load_records(src):
-    """(records, from_file); records are (id, seq, constrain) (cli.py:88-105)."""
+def _read_lines(numbered: Iterable[Tuple[int, str]]) -> List[Record]:
+    return [Record(lineno, text.strip().upper()) for lineno, text in numbered if text.strip()]
+
+
+_READERS = {"{": _read_jsonl, ">": _read_fasta}
+
+
+def load_records(src: str):
+    """(records, from_file): the records (id, seq, constrain) named by `src`,
+    a file path or a literal sequence (input behaviour above)."""
     if os.path.isfile(src):
-        head = ""
         with open(src) as fh:
-            for line in fh:
-                if line.strip():
-                    head = line.strip()[0]
-                    break
-        if head == "{":
-            return _parse_jsonl(src), True
-        if head == ">":
-            return _parse_fasta(src), True
-        return _parse_seq_lines(src), True
+            numbered = [(k, line.rstrip("\n")) for k, line in enumerate(fh)]
+        first = next((t.strip()[0] for _, t in numbered if t.strip()), "")
+        return _READERS.get(first, _read_lines)(numbered), True
     seq = src.strip().upper()
-    if seq and all(c in _SEQ_CHARS for c in seq):
-        return [(0, seq, None)], False
+    if seq and frozenset(seq) <= _NUCLEOTIDES:
+        return [Record(0, seq)], False
     raise SystemExit(f"'{src}' is not an existing file nor a valid RNA sequence (ACGUTN)")
 
 
-def build_mask(seq, constrain, where=""):
-    """Per-base 0/1 mask (1 = forced unpaired) -> int8 array, or None (cli.py:108-124)."""
-    if not constrain:
+def build_mask(seq: str, constrain, where: str = ""):
+    """int8 forced-unpaired mask (1 = forced) from a record's "constrain", or
+    None when it has none (input behaviour above)."""
+    if constrain is None or len(constrain) == 0:
         return None
-    L = len(seq)
-    bits = [1 if c == "1" else 0 for c in constrain] if isinstance(constrain, str) else list(constrain)
-    if len(bits) != L:
-        raise SystemExit(f"{where}constrain length {len(bits)} != seq length {L}")
-    m = np.zeros(L, np.int8)
-    for i, b in enumerate(bits):
-        if b not in (0, 1):
-            raise SystemExit(f"{where}constrain[{i}] = {b!r}, expected 0 or 1")
-        m[i] = b
-    return m
+    if isinstance(constrain, str):
+        bits = [int(ch == "1") for ch in constrain]
+    else:
+        bits = list(constrain)
+    if len(bits) != len(seq):
+        raise SystemExit(f"{where}constrain length {len(bits)} != seq length {len(seq)}")
+    bad = next((k for k, b in enumerate(bits) if b not in (0, 1)), None)
+    if bad is not None:
+        raise SystemExit(f"{where}constrain[{bad}] = {bits[bad]!r}, expected 0 or 1")
+    return np.asarray(bits, np.int8)
 
 
 def fold(records, P, mode="mea", sample_n=0, with_logz=False, gamma=6.0, chunk=4096, seed=0):

@@ -8,8 +8,11 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <numeric>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -85,6 +88,112 @@ int64_t arena_words(Job job, int L) {
     }
 }
 
+// One row of the schedule table (cf_engine_load_tuning): a batch matches
+// when all its conditions hold; the first matching row decides the schedule
+// of the automatic batched path.
+struct TuneRow {
+    int min_len = 0, max_len = CF_MAX_LEN;   // shortest >= min_len, longest <= max_len
+    int min_batch = 0, max_batch = 0;        // n >= min_batch, n <= max_batch (0 = no limit)
+    int uniform = -1;                        // 1: lengths within 25 %, 0: mixed, -1: either
+    unsigned jobs = 0;                       // bit per Job (0 = every job)
+    int sched = 3;                           // 1 warp, 2 cta, 3 group, 4 cluster
+    int group = 0;                           // sequences per CTA for the grouped kernels (0 = automatic)
+    int ctas = 0;                            // resident CTAs per SM of the CTA kernel (0 = automatic)
+};
+
+// The built-in table (GB300, contrafold_gpu_gb300/autotune.py sweeps):
+//  * small batches of long sequences fold on a thread-block cluster each (one
+//    600-nt MEA fold 172 -> 144 ms, 1,000 nt 450 -> 297 ms; 64 x 300 nt stays
+//    grouped: 69 vs 125 ms): every sequence >= 512 nt and at most two
+//    clusters' CTAs per SM (38 sequences on 152 SMs);
+//  * large batches of mixed short lengths take the warp-per-sequence kernel
+//    (200 nt: n=1024 warp 8.7k vs grouped 10.2k MEA folds/s, n=2048 15.1k vs
+//    13.3k; 60 nt: n=2048 172k vs 186k, n=4096 238k vs 191k);
+//  * everything else folds grouped (lengths within 25 %: one wave of full
+//    CTAs; mixed: several waves).
+std::vector<TuneRow> default_tuning() {
+    const unsigned lbms = (1u << JOB_LOGZ) | (1u << JOB_BPP) | (1u << JOB_MEA) | (1u << JOB_SAMPLE);
+    const unsigned lbm = (1u << JOB_LOGZ) | (1u << JOB_BPP) | (1u << JOB_MEA);
+    std::vector<TuneRow> t(4);
+    t[0].min_len = 512; t[0].min_batch = 1; t[0].max_batch = 38; t[0].jobs = lbms; t[0].sched = 4;
+    t[1].max_len = 80; t[1].min_batch = 4096; t[1].uniform = 0; t[1].jobs = lbm; t[1].sched = 1;
+    t[2].max_len = 80; t[2].uniform = 0; t[2].jobs = lbm; t[2].sched = 3;
+    t[3].max_len = 256; t[3].min_batch = 2048; t[3].uniform = 0; t[3].jobs = lbm; t[3].sched = 1;
+    return t;
+}
+
+// Parses a schedule table: one row per line, '#' starts a comment,
+//   min_len max_len min_batch max_batch uniform jobs schedule group ctas_per_sm
+// uniform: any | uniform | mixed; jobs: all or a comma list of logz, logz64,
+// bpp, mea, mfe, sample; schedule: warp | cta | group | cluster.
+int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err) {
+    std::string line;
+    int ln = 0;
+    rows.clear();
+    while (std::getline(in, line)) {
+        ++ln;
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        std::istringstream ls(line);
+        std::string f[9];
+        int nf = 0;
+        while (nf < 9 && (ls >> f[nf])) ++nf;
+        if (nf == 0) continue;
+        std::string extra;
+        if (nf < 9 || (ls >> extra)) {
+            err = "line " + std::to_string(ln) + ": expected 9 fields";
+            return CF_EINVAL;
+        }
+        TuneRow r;
+        auto num = [&](const std::string& x, int lo, int hi, int& out) {
+            char* end = nullptr;
+            const long v = std::strtol(x.c_str(), &end, 10);
+            if (end == x.c_str() || *end != 0 || v < lo || v > hi) return false;
+            out = (int)v;
+            return true;
+        };
+        if (!num(f[0], 0, CF_MAX_LEN, r.min_len) || !num(f[1], 0, CF_MAX_LEN, r.max_len) ||
+            !num(f[2], 0, 1 << 30, r.min_batch) || !num(f[3], 0, 1 << 30, r.max_batch) ||
+            !num(f[7], 0, cf::kMaxGroup, r.group) || !num(f[8], 0, 64, r.ctas)) {
+            err = "line " + std::to_string(ln) + ": bad number";
+            return CF_EINVAL;
+        }
+        if (f[4] == "any") r.uniform = -1;
+        else if (f[4] == "uniform") r.uniform = 1;
+        else if (f[4] == "mixed") r.uniform = 0;
+        else { err = "line " + std::to_string(ln) + ": uniform must be any, uniform or mixed"; return CF_EINVAL; }
+        if (f[5] != "all") {
+            std::istringstream js(f[5]);
+            std::string j;
+            while (std::getline(js, j, ',')) {
+                static const char* names[] = {"logz", "logz64", "bpp", "mea", "mfe", "sample"};
+                int k = 0;
+                while (k < 6 && j != names[k]) ++k;
+                if (k == 6) { err = "line " + std::to_string(ln) + ": unknown job '" + j + "'"; return CF_EINVAL; }
+                r.jobs |= 1u << k;   // the Job enum's order
+            }
+        }
+        static const char* scheds[] = {"warp", "cta", "group", "cluster"};
+        int k = 0;
+        while (k < 4 && f[6] != scheds[k]) ++k;
+        if (k == 4) { err = "line " + std::to_string(ln) + ": unknown schedule '" + f[6] + "'"; return CF_EINVAL; }
+        r.sched = k + 1;
+        rows.push_back(r);
+    }
+    return CF_OK;
+}
+
+const TuneRow* match_tuning(const std::vector<TuneRow>& rows, Job job, int n, int Lmin, int Lmax, bool uniform) {
+    for (const TuneRow& r : rows) {
+        if (Lmin < r.min_len || Lmax > r.max_len || n < r.min_batch) continue;
+        if (r.max_batch > 0 && n > r.max_batch) continue;
+        if (r.uniform >= 0 && (r.uniform == 1) != uniform) continue;
+        if (r.jobs != 0 && !(r.jobs & (1u << job))) continue;
+        return &r;
+    }
+    return nullptr;
+}
+
 }  // namespace
 
 struct cf_engine {
@@ -111,28 +220,13 @@ struct cf_engine {
     int ctas_per_sm = 0; // CTA-persistent occupancy cap (0 = auto)
     int group = 0;       // sequences per CTA of the grouped kernels (0 = auto)
     size_t smem_optin = 0;
+    std::vector<TuneRow> tuning = default_tuning();   // schedule table of the automatic path
 };
 
 namespace {
 
-// ---- group-size autotune table: sequences per CTA by length range ----
-// Chosen by the in-tree tuner (contrafold_gpu_gb300/autotune.py) on GB300.
-// Batched-path schedule (GB300 tuning, autotune.py --batch-sizes): batches of
-// at least auto_warp_min_batch() sequences, none longer than
-// auto_warp_max_len(), take the warp-per-sequence kernel (throughput); smaller
-// batches fold one sequence per CTA (latency: a single 250-nt MEA fold takes
-// 56 ms on a CTA, 232 ms on a warp).  Measured crossover (MEA folds/s, warp vs
-// grouped): 200 nt n=1024 8.7k vs 10.2k, n=2048 15.1k vs 13.3k; 60 nt n=2048
-// 172k vs 186k, n=4096 238k vs 191k.
-int auto_warp_max_len() { return 256; }
-int auto_warp_min_batch(int Lmax) { return Lmax <= 80 ? 4096 : 2048; }
-// Small batches of long sequences fold on a thread-block cluster each
-// (GB300, MEA: one 600-nt fold 172 -> 144 ms, 1,000 nt 450 -> 297 ms,
-// 32 x 600 nt 184 -> 158 ms; 64 x 300 nt stays grouped: 69 vs 125 ms).
-int auto_cluster_min_len() { return 512; }
-// CTAs per SM of the persistent CTA kernel by length.
-int auto_ctas_per_sm(int Lmax) { return Lmax <= 160 ? 4 : 3; }
-
+// Sequences per CTA of the grouped kernels for mixed lengths, by the median
+// length (autotune.py --groups on GB300).
 int group_for_length(int L) {
     if (L <= 64) return 8;
     if (L <= 160) return 4;
@@ -220,15 +314,17 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // Mixed lengths stay one plan, longest first: splitting a 40-400 nt batch
     // at 256 nt into a warp-kernel part and a grouped part on two streams was
     // slower for every job (MEA 8.5k vs 10.7k folds/s).
-    if (sched == 0 && batched && Lmin >= auto_cluster_min_len() &&
-        (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE)) {
-        int sms = 0;
-        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
-        if ((int64_t)n * cf::kClusterCtas <= (int64_t)cf::kClusterMinBlocks * sms) sched = 4;
+    int row_ctas = 0;
+    if (sched == 0) {   // the schedule table decides (cf_engine_load_tuning)
+        sched = 3;
+        if (batched) {
+            if (const TuneRow* r = match_tuning(eng->tuning, job, n, Lmin, P.Lmax, uniform)) {
+                sched = r->sched;
+                row_ctas = r->ctas;
+                if (r->group > 0 && eng->group == 0) P.group = r->group;
+            }
+        }
     }
-    if (sched == 0)
-        sched = (job != JOB_SAMPLE && !uniform && P.Lmax <= auto_warp_max_len() && n >= auto_warp_min_batch(P.Lmax))
-                    ? 1 : 3;
     P.cluster = batched && sched == 4 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
     if (P.cluster) P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group) : 1;
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
@@ -242,7 +338,8 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
         per_sm = std::max(per_sm, 1);
         if (eng->ctas_per_sm > 0) per_sm = std::min(per_sm, eng->ctas_per_sm);
-        else per_sm = std::min(per_sm, auto_ctas_per_sm(P.Lmax));
+        else if (row_ctas > 0) per_sm = std::min(per_sm, row_ctas);
+        else per_sm = std::min(per_sm, P.Lmax <= 160 ? 4 : 3);   // GB300: 4 up to 160 nt
         int64_t grid = std::min<int64_t>((int64_t)per_sm * sms, n);
         P.slot_words = cf::arena32(P.Lmax).total;
         while (grid > 1 && grid * P.slot_words > budget_words) --grid;
@@ -725,6 +822,11 @@ int cf_engine_create(const float* params32, const double* params64, int device, 
         return fail(CF_ECUDA, "cudaStreamCreate failed");
     }
     int rc = cf_engine_set_params(e, params32, params64);
+    if (!rc) {
+        // a schedule table written by the tuner, when the environment names one
+        const char* tf = std::getenv("CONTRAFOLD_GB300_TUNING");
+        if (tf && *tf) rc = cf_engine_load_tuning(e, tf);
+    }
     if (rc) {
         cf_engine_destroy(e);
         return rc;
@@ -786,6 +888,23 @@ int cf_engine_set_group(cf_engine* e, int group) {
     e->group = group;
     return CF_OK;
 }
+
+int cf_engine_load_tuning(cf_engine* e, const char* path) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    if (!path) {
+        e->tuning = default_tuning();
+        return CF_OK;
+    }
+    std::ifstream in(path);
+    if (!in) return fail(CF_EINVAL, std::string("cannot read tuning table ") + path);
+    std::vector<TuneRow> rows;
+    std::string err;
+    if (parse_tuning(in, rows, err)) return fail(CF_EINVAL, std::string(path) + ": " + err);
+    e->tuning = rows;
+    return CF_OK;
+}
+
+int cf_engine_tuning_rows(const cf_engine* e) { return e ? (int)e->tuning.size() : 0; }
 
 int cf_logz(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
             float* logz_out) {

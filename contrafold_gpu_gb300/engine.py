@@ -26,7 +26,8 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
+           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_engine_load_tuning",
+           "cf_engine_tuning_rows", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group", "cf_plan_set_graph", "cf_plan_schedule", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
@@ -63,6 +64,8 @@ def load_library(path: str = LIB_PATH):
         L.cf_engine_set_mode.argtypes = [vp, ctypes.c_int]
         L.cf_engine_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.cf_engine_set_group.argtypes = [vp, ctypes.c_int]
+        L.cf_engine_load_tuning.argtypes = [vp, ctypes.c_char_p]
+        L.cf_engine_tuning_rows.argtypes = [vp]
         L.cf_last_error.restype = ctypes.c_char_p
         L.cf_version.restype = ctypes.c_char_p
         L.cf_logz.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f32p]
@@ -88,7 +91,8 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_schedule.argtypes = [vp]
         L.cf_plan_schedule.restype = ctypes.c_char_p
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
+                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_engine_load_tuning",
+                     "cf_engine_tuning_rows", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
                      "cf_sample_seeded", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group", "cf_plan_set_graph"):
             getattr(L, name).restype = ctypes.c_int
@@ -188,6 +192,15 @@ class Engine:
 
     def set_budget(self, nbytes: int):
         self._check(self.lib.cf_engine_set_budget(self._h, int(nbytes)))
+
+    def load_tuning(self, path: Optional[str] = None):
+        """Schedule table of the automatic batched path, as written by
+        `autotune --write-table` (None restores the built-in table)."""
+        self._check(self.lib.cf_engine_load_tuning(self._h, None if path is None else os.fsencode(path)))
+
+    @property
+    def tuning_rows(self) -> int:
+        return int(self.lib.cf_engine_tuning_rows(self._h))
 
     # ---- batch entry points ----
     def _args(self, B: Batch):

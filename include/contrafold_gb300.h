@@ -107,6 +107,25 @@ int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
  * 0 = automatic (by the median length, capped to keep two CTAs per SM).  The
  * tuner's knob; results are identical for every value. */
 int cf_engine_set_group(cf_engine* eng, int group);
+/* Schedule table of the automatic batched path (schedule kind 0), written by
+ * the tuner (python -m contrafold_gpu_gb300.autotune --write-table FILE).
+ * One row per line, '#' starts a comment:
+ *   min_len max_len min_batch max_batch uniform jobs schedule group ctas_per_sm
+ * A batch matches a row when its shortest sequence has >= min_len nt, its
+ * longest <= max_len, its size is in [min_batch, max_batch] (max_batch 0 = no
+ * limit), its lengths are all within 25 % of each other (uniform = "uniform"),
+ * or not ("mixed"), or either ("any"), and its job is in `jobs` ("all" or a
+ * comma list of logz, logz64, bpp, mea, mfe, sample).  The first matching row
+ * gives the schedule (warp, cta, group or cluster), the sequences per CTA of
+ * the grouped kernels and the CTAs per SM of the CTA kernel (0 = automatic);
+ * a batch no row matches folds grouped.  path NULL restores the built-in
+ * table; cf_engine_create loads the file named by the environment variable
+ * CONTRAFOLD_GB300_TUNING when it is set.  A malformed file is CF_EINVAL and
+ * leaves the table unchanged.  No reference counterpart (the reference has
+ * one launch shape).  Results are identical for every table. */
+int cf_engine_load_tuning(cf_engine* eng, const char* path);
+/* Rows of the engine's schedule table. */
+int cf_engine_tuning_rows(const cf_engine* eng);
 
 const char* cf_last_error(void);
 const char* cf_version(void);

@@ -90,23 +90,56 @@ def binom_quantile(K, q, tail):
     return 0
 
 
+def binom_upper_tail(N, p, c):
+    """P(Binomial(N, p) >= c), summed from the pmf (c small)."""
+    import math
+    if c <= 0:
+        return 1.0
+    if p <= 0.0:
+        return 0.0
+    lp, lq = math.log(p), math.log1p(-p)
+    tot, x = 0.0, c
+    while x <= N:
+        t = math.exp(math.lgamma(N + 1) - math.lgamma(x + 1) - math.lgamma(N - x + 1) + x * lp + (N - x) * lq)
+        tot += t
+        if x > c + 10 and t < 1e-18 * max(tot, 1e-300):
+            break
+        x += 1
+    return min(1.0, tot)
+
+
 def check_pair_frequencies(samples, p, n):
-    """Per pair: |f - p| <= 3 sqrt(p (1 - p) / N) + 1/N.  Pairs are many (up to
-    L^2 / 2), and a 3-sigma band holds for ~99.7 % of them by construction, so
-    the test allows as many exceedances as a Binomial(K, 0.003) stays under
-    with probability 1 - 1e-6 (K = pairs with p >= 1/N, the only ones that can
-    leave the band), and none beyond 5 sigma + 1/N."""
+    """Sampled pair frequencies f against pair probabilities p, N = n samples.
+
+    Pairs with N p >= 10 (where the binomial count is close to normal): per
+    pair |f - p| <= 3 sqrt(p (1 - p) / N) + 1/N.  A 3-sigma band holds for
+    ~99.7 % of pairs by construction, so as many exceedances are allowed as a
+    Binomial(K, 0.003) stays under with probability 1 - 1e-6 (K = such pairs),
+    and none beyond 5 sigma + 1/N.
+    Pairs with N p < 10 (Poisson regime: the normal band would understate the
+    upper tail): the observed count c must have an upper-tail probability
+    P(Binomial(N, p) >= c) >= 1e-6 / K_small (Bonferroni over the K_small such
+    pairs seen), and a pair of probability 0 is never drawn.
+    Returns (3-sigma exceedances, K)."""
     L = p.shape[0]
-    f = np.zeros((L, L))
+    cnt = np.zeros((L, L))
     for db in samples:
         for x, y in pairs_of(db):
-            f[x, y] += 1
-    f /= n
+            cnt[x, y] += 1
+    f = cnt / n
+    normal = n * p >= 10
     sig = np.sqrt(p * (1 - p) / n)
-    out3 = np.abs(f - p) > 3 * sig + 1.0 / n
-    out5 = np.abs(f - p) > 5 * sig + 1.0 / n
-    K = int(np.count_nonzero(p >= 1.0 / n))
+    out3 = normal & (np.abs(f - p) > 3 * sig + 1.0 / n)
+    out5 = normal & (np.abs(f - p) > 5 * sig + 1.0 / n)
+    K = int(np.count_nonzero(normal))
     allowed = binom_quantile(K, 0.003, 1e-6)
-    assert int(out5.sum()) == 0, np.argwhere(out5)[:5]
+    assert int(out5.sum()) == 0, [(int(a), int(b), float(f[a, b]), float(p[a, b])) for a, b in np.argwhere(out5)[:5]]
     assert int(out3.sum()) <= allowed, (int(out3.sum()), allowed, K)
+    impossible = (p == 0) & (cnt > 0)
+    assert not impossible.any(), np.argwhere(impossible)[:5]
+    small = np.argwhere(~normal & (cnt > 0) & (p > 0))
+    thr = 1e-6 / max(1, len(small))
+    for a, b in small:
+        tail = binom_upper_tail(n, float(p[a, b]), int(cnt[a, b]))
+        assert tail >= thr, (int(a), int(b), int(cnt[a, b]), float(p[a, b]), tail)
     return int(out3.sum()), K

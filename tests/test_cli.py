@@ -35,6 +35,24 @@ def test_jsonl_errors(tmp_path):
         cli.load_records(str(bad))
 
 
+def test_input_behaviour_edges(tmp_path):
+    """A FASTA record without sequence is dropped (and does not count for the
+    next unnamed header); a JSON line that is not an object has no 'seq';
+    leading blank lines do not decide the format; any character but '1' in a
+    constrain string is 0."""
+    f = tmp_path / "e.fa"
+    f.write_text("\n\n>empty\n>\nGG CC \n\n>z\nau\n")
+    assert cli.load_records(str(f))[0] == [(0, "GG CC", None), ("z", "AU", None)]
+    j = tmp_path / "e.jsonl"
+    j.write_text('\n{"seq": "GGGAAACCC", "id": 7}\n[1, 2]\n')
+    with pytest.raises(SystemExit, match="line 2: missing required field"):
+        cli.load_records(str(j))
+    assert cli.build_mask("ACGU", "01x1").tolist() == [0, 1, 0, 1]
+    assert cli.build_mask("ACGU", "") is None and cli.build_mask("ACGU", []) is None
+    with pytest.raises(SystemExit):
+        cli.load_records("ACGX")
+
+
 def test_build_mask():
     assert cli.build_mask("ACGU", None) is None
     assert cli.build_mask("ACGU", "0101").tolist() == [0, 1, 0, 1]
