@@ -19,6 +19,7 @@
 #include "../../include/contrafold_gb300.h"
 #include "cf_host.h"
 #include "cf_kernels.h"
+#include "cf_queue.h"
 #include "cf_sample.h"
 #include "cf_warp.h"
 
@@ -96,8 +97,8 @@ struct TuneRow {
     int min_batch = 0, max_batch = 0;        // n >= min_batch, n <= max_batch (0 = no limit)
     int uniform = -1;                        // 1: lengths within 25 %, 0: mixed, -1: either
     unsigned jobs = 0;                       // bit per Job (0 = every job)
-    int sched = 3;                           // 1 warp, 2 cta, 3 group, 4 cluster
-    int group = 0;                           // sequences per CTA for the grouped kernels (0 = automatic)
+    int sched = 3;                           // 1 warp, 2 cta, 3 group, 4 cluster, 5 queue
+    int group = 0;                           // sequences per CTA: grouped kernels / queue seats (0 = automatic)
     int ctas = 0;                            // resident CTAs per SM of the CTA kernel (0 = automatic)
 };
 
@@ -125,7 +126,7 @@ std::vector<TuneRow> default_tuning() {
 // Parses a schedule table: one row per line, '#' starts a comment,
 //   min_len max_len min_batch max_batch uniform jobs schedule group ctas_per_sm
 // uniform: any | uniform | mixed; jobs: all or a comma list of logz, logz64,
-// bpp, mea, mfe, sample; schedule: warp | cta | group | cluster.
+// bpp, mea, mfe, sample; schedule: warp | cta | group | cluster | queue.
 int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err) {
     std::string line;
     int ln = 0;
@@ -154,7 +155,7 @@ int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err)
         };
         if (!num(f[0], 0, CF_MAX_LEN, r.min_len) || !num(f[1], 0, CF_MAX_LEN, r.max_len) ||
             !num(f[2], 0, 1 << 30, r.min_batch) || !num(f[3], 0, 1 << 30, r.max_batch) ||
-            !num(f[7], 0, cf::kMaxGroup, r.group) || !num(f[8], 0, 64, r.ctas)) {
+            !num(f[7], 0, cf::kQueueMaxSeats, r.group) || !num(f[8], 0, 64, r.ctas)) {
             err = "line " + std::to_string(ln) + ": bad number";
             return CF_EINVAL;
         }
@@ -173,10 +174,10 @@ int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err)
                 r.jobs |= 1u << k;   // the Job enum's order
             }
         }
-        static const char* scheds[] = {"warp", "cta", "group", "cluster"};
+        static const char* scheds[] = {"warp", "cta", "group", "cluster", "queue"};
         int k = 0;
-        while (k < 4 && f[6] != scheds[k]) ++k;
-        if (k == 4) { err = "line " + std::to_string(ln) + ": unknown schedule '" + f[6] + "'"; return CF_EINVAL; }
+        while (k < 5 && f[6] != scheds[k]) ++k;
+        if (k == 5) { err = "line " + std::to_string(ln) + ": unknown schedule '" + f[6] + "'"; return CF_EINVAL; }
         r.sched = k + 1;
         rows.push_back(r);
     }
@@ -212,6 +213,7 @@ struct cf_engine {
     DevBuf<int> status;
     DevBuf<char> samples;
     DevBuf<uint64_t> seeds;
+    DevBuf<int32_t> stream_idx;
     DevBuf<float> bonus;
     DevBuf<double> counts, unpaired;
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
@@ -241,6 +243,8 @@ struct Plan {
     bool cta = false;             // persistent CTA-per-sequence fused kernel (batched path)
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
     bool cluster = false;         // a thread-block cluster per group (latency of long sequences)
+    bool queue = false;           // dataflow schedule: one persistent launch, warps pulling (sequence, step, chunk)
+    int seats = 0;                // its sequences in progress per CTA
     int wgrid = 0;                // its grid
     int64_t slot_words = 0;       // its arena slot per warp
     std::vector<SeqDesc> descs;   // grouped order
@@ -314,19 +318,50 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     // Mixed lengths stay one plan, longest first: splitting a 40-400 nt batch
     // at 256 nt into a warp-kernel part and a grouped part on two streams was
     // slower for every job (MEA 8.5k vs 10.7k folds/s).
-    int row_ctas = 0;
+    int row_ctas = 0, row_group = 0;
     if (sched == 0) {   // the schedule table decides (cf_engine_load_tuning)
         sched = 3;
         if (batched) {
             if (const TuneRow* r = match_tuning(eng->tuning, job, n, Lmin, P.Lmax, uniform)) {
                 sched = r->sched;
                 row_ctas = r->ctas;
-                if (r->group > 0 && eng->group == 0) P.group = r->group;
+                row_group = r->group;
+                if (r->group > 0 && eng->group == 0 && sched == 3) P.group = r->group;
             }
         }
     }
     P.cluster = batched && sched == 4 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
     if (P.cluster) P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group) : 1;
+    P.queue = batched && sched == 5 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
+    if (P.queue) {
+        // sequences in progress per CTA: enough open chunks for the 8 warps on
+        // short sequences, fewer (less L2 working set) on long ones
+        int seats = eng->group > 0 ? eng->group : row_group > 0 ? row_group
+                  : P.Lmax <= 320 ? 8 : P.Lmax <= 640 ? 4 : 2;
+        seats = std::max(1, std::min(seats, cf::kQueueMaxSeats));
+        const int mode = job == JOB_LOGZ ? cf::kQueueLogZ : job == JOB_MEA ? cf::kQueueMea
+                       : job == JOB_BPP ? cf::kQueueBpp : cf::kQueueSample;
+        const size_t smem = cf::queue_smem_bytes(P.Lmax, seats, mode);
+        int rc = ensure_smem(eng, smem);
+        if (rc) return rc;
+        int per_sm = 0, sms = 0;
+        CF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cf::queue_kernel(mode), cf::kQueueThreads, smem));
+        CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
+        if (eng->ctas_per_sm > 0) per_sm = std::min(per_sm, eng->ctas_per_sm);
+        else if (row_ctas > 0) per_sm = std::min(per_sm, row_ctas);
+        int64_t grid = std::min<int64_t>((int64_t)std::max(per_sm, 1) * sms, (n + seats - 1) / seats);
+        P.slot_words = cf::queue_slot_words(P.Lmax);
+        while (grid > 1 && grid * seats * P.slot_words > budget_words) --grid;
+        if (grid * seats * P.slot_words <= budget_words) {
+            P.wgrid = (int)std::max<int64_t>(grid, 1);
+            P.seats = seats;
+            P.group = 1;
+            P.slice_begin = {0, n};
+            P.slice_words = {grid * seats * P.slot_words};
+            return CF_OK;
+        }
+        P.queue = false;   // not even one CTA of seats fits: per-sequence kernels, sliced
+    }
     P.cta = batched && sched == 2 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA);
     if (P.cta) {
         const int mode = job == JOB_LOGZ ? cf::kCtaLogZ : job == JOB_MEA ? cf::kCtaMea : cf::kCtaBpp;
@@ -439,6 +474,8 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
         CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     for (int mode = 0; mode < 3; ++mode)
         CF_CUDA(cudaFuncSetAttribute(cf::cta_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (int mode = 0; mode < 4; ++mode)
+        CF_CUDA(cudaFuncSetAttribute(cf::queue_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     const cf::ClusterKernels ck = cf::cluster_kernels();
     for (cf::FoldKernel k : {ck.mea, ck.bpp, ck.inside_acc})
         CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -495,6 +532,7 @@ struct SampleJob {
     int n_samples = 0;
     uint64_t seed = 0;
     const uint64_t* d_seeds = nullptr;   // per-sequence seeds (cf_sample_seeded) or null
+    const int32_t* d_stream = nullptr;   // per-sequence Philox sequence index (cf_sample_tasks) or null
     char* d_out = nullptr;
 };
 
@@ -554,6 +592,38 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         CF_PHASE(0, (cudaLaunchKernel(cf::cta_kernel(mode), dim3(P.wgrid), dim3(cf::kFoldThreads), args, smem, st)));
         return CF_OK;
     }
+    if (P.queue) {
+        cf::QueueArgs Q;
+        Q.descs = X.d_descs;
+        Q.n = n;
+        Q.Lmax = P.Lmax;
+        Q.seats = P.seats;
+        Q.seqs = d_seqs;
+        Q.mask = d_mask;
+        Q.blob32 = eng->blob32.p;
+        Q.ws = X.arena;
+        Q.slot_words = P.slot_words;
+        Q.counter = X.status + 1;
+        Q.gamma = gamma;
+        Q.logz = d_logz;
+        Q.structs = d_structs;
+        Q.post_out = d_post;
+        Q.post_offs = d_post_offs;
+        Q.n_samples = sj ? sj->n_samples : 0;
+        Q.seed = sj ? sj->seed : 0;
+        Q.seeds = sj ? sj->d_seeds : nullptr;
+        Q.stream_idx = sj ? sj->d_stream : nullptr;
+        Q.out = sj ? sj->d_out : nullptr;
+        Q.status = X.status;
+        const int mode = job == JOB_LOGZ ? cf::kQueueLogZ : job == JOB_MEA ? cf::kQueueMea
+                       : job == JOB_BPP ? cf::kQueueBpp : cf::kQueueSample;
+        const size_t smem = cf::queue_smem_bytes(P.Lmax, P.seats, mode);
+        if ((rc = ensure_smem(eng, smem))) return rc;
+        CF_CUDA(cudaMemsetAsync(X.status + 1, 0, sizeof(int), st));
+        void* args[] = {&Q};
+        CF_PHASE(0, (cudaLaunchKernel(cf::queue_kernel(mode), dim3(P.wgrid), dim3(cf::kQueueThreads), args, smem, st)));
+        return CF_OK;
+    }
     if (P.warp) {
         cf::WarpArgs W;
         W.descs = X.d_descs;
@@ -573,6 +643,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         W.n_samples = sj ? sj->n_samples : 0;
         W.seed = sj ? sj->seed : 0;
         W.seeds = sj ? sj->d_seeds : nullptr;
+        W.stream_idx = sj ? sj->d_stream : nullptr;
         W.out = sj ? sj->d_out : nullptr;
         W.status = X.status;
         const int mode = job == JOB_LOGZ ? cf::kWarpLogZ : job == JOB_MEA ? cf::kWarpMea
@@ -682,6 +753,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                 S.Lmax = P.Lmax;
                 S.seed = sj->seed;
                 S.seeds = sj->d_seeds;
+                S.stream_idx = sj->d_stream;
                 S.seqs = d_seqs;
                 S.mask = d_mask;
                 S.blob32 = eng->blob32.p;
@@ -717,7 +789,7 @@ int read_status(cf_engine* eng, cudaStream_t st) {
 int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask,
              int32_t n, float gamma, float* logz_out, double* logz64_out, char* struct_out,
              const int64_t* post_offsets, float* post_out, int n_samples = 0, uint64_t seed = 0,
-             char* sample_out = nullptr, const uint64_t* seeds = nullptr) {
+             char* sample_out = nullptr, const uint64_t* seeds = nullptr, const int32_t* stream_idx = nullptr) {
     int rc = check_batch(eng, seqs, offsets, n);
     if (rc) return rc;
     if (n == 0) return CF_OK;
@@ -775,6 +847,11 @@ int run_host(cf_engine* eng, Job job, const uint8_t* seqs, const int64_t* offset
             if ((rc = eng->seeds.ensure(n))) return rc;
             CF_CUDA(cudaMemcpyAsync(eng->seeds.p, seeds, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
             sj.d_seeds = eng->seeds.p;
+        }
+        if (stream_idx) {
+            if ((rc = eng->stream_idx.ensure(n))) return rc;
+            CF_CUDA(cudaMemcpyAsync(eng->stream_idx.p, stream_idx, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+            sj.d_stream = eng->stream_idx.p;
         }
     }
     if ((rc = eng->descs.ensure(n))) return rc;
@@ -841,7 +918,7 @@ int cf_engine_destroy(cf_engine* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->blob32.release(); e->blob64.release(); e->arena.release(); e->seqs.release(); e->mask.release();
     e->descs.release(); e->logz.release(); e->logz64.release(); e->structs.release(); e->post.release();
-    e->post_offs.release(); e->status.release(); e->samples.release(); e->seeds.release();
+    e->post_offs.release(); e->status.release(); e->samples.release(); e->seeds.release(); e->stream_idx.release();
     e->bonus.release(); e->counts.release(); e->unpaired.release();
 
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -876,7 +953,7 @@ int cf_engine_set_mode(cf_engine* e, int mode) {
 
 int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
-    if (kind < 0 || kind > 4 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
+    if (kind < 0 || kind > 5 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
     e->sched = kind;
     e->ctas_per_sm = ctas_per_sm;
     return CF_OK;
@@ -884,7 +961,7 @@ int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
 
 int cf_engine_set_group(cf_engine* e, int group) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
-    if (group < 0 || group > cf::kMaxGroup) return fail(CF_EINVAL, "group must be in [0, 32]");
+    if (group < 0 || group > cf::kQueueMaxSeats) return fail(CF_EINVAL, "group must be in [0, 64]");
     e->group = group;
     return CF_OK;
 }
@@ -951,6 +1028,30 @@ int cf_sample_seeded(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, 
     if (n > 0 && n_samples > 0 && (!out || !seeds)) return fail(CF_EINVAL, "out / seeds is NULL");
     return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, n_samples,
                     0, out, seeds);
+}
+
+int cf_sample_tasks(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
+                    int32_t chunk, uint64_t seed, char* out) {
+    if (chunk <= 0) return fail(CF_EINVAL, "chunk must be > 0");
+    if (n > 0 && !out) return fail(CF_EINVAL, "out is NULL");
+    int rc = check_batch(e, seqs, offsets, n);
+    if (rc) return rc;
+    // the reference's order: tasks sorted by length (stable), cut into chunks;
+    // chunk c0 samples with seed + c0, its k-th task with sequence index k
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return offsets[x + 1] - offsets[x] < offsets[y + 1] - offsets[y];
+    });
+    std::vector<uint64_t> seeds(n);
+    std::vector<int32_t> sidx(n);
+    for (int r = 0; r < n; ++r) {
+        const int c0 = r - r % chunk;
+        seeds[order[r]] = seed + (uint64_t)c0;
+        sidx[order[r]] = r - c0;
+    }
+    return run_host(e, JOB_SAMPLE, seqs, offsets, mask, n, 0.f, nullptr, nullptr, nullptr, nullptr, nullptr, 1, 0, out,
+                    seeds.data(), sidx.data());
 }
 
 }  // extern "C"
@@ -1053,6 +1154,10 @@ int plan_prepare_smem(cf_engine* e, Job job, const Plan& P) {
         bytes = cf::fold_smem_bytes(P.Lmax, 1, false);
     } else if (P.warp) {
         bytes = cf::warp_smem_bytes(P.Lmax);
+    } else if (P.queue) {
+        const int mode = job == JOB_LOGZ ? cf::kQueueLogZ : job == JOB_MEA ? cf::kQueueMea
+                       : job == JOB_BPP ? cf::kQueueBpp : cf::kQueueSample;
+        bytes = cf::queue_smem_bytes(P.Lmax, P.seats, mode);
     } else {
         const bool fp64 = job == JOB_LOGZ64 || job == JOB_MFE;
         bytes = std::max(cf::fold_smem_bytes(P.Lmax, P.group, fp64), cf::plain_smem_bytes(P.Lmax));
@@ -1181,6 +1286,7 @@ const char* cf_plan_schedule(const cf_plan* p) {
     if (p->P.warp) return "warp";
     if (p->P.cta) return "cta";
     if (p->P.cluster) return "cluster";
+    if (p->P.queue) return "queue";
     return "group";
 }
 

@@ -217,6 +217,7 @@ extern "C" int cf_mea_scratch(cf_engine* e, const uint8_t* seqs, const int64_t* 
     W.n_samples = 0;
     W.seed = 0;
     W.seeds = nullptr;
+    W.stream_idx = nullptr;
     W.out = nullptr;
     W.status = status;
     void* args[] = {&W};

@@ -59,11 +59,12 @@ __global__ void __launch_bounds__(kSampleWarps * 32) k_sample32(SampleArgs A) {
         X.T.FC = base + ar.FC; X.T.FM = base + ar.FM; X.T.FM1 = base + ar.FM1; X.T.F5 = base + ar.F5;
         X.T.m = L + 1;
         X.T.sized(L);
+        const int sidx = A.stream_idx != nullptr ? A.stream_idx[D.idx] : (A.seeds != nullptr ? 0 : D.idx);
         if (A.seeds != nullptr) {
             const uint64_t sd = A.seeds[D.idx];
-            sample_one(X, smp, 0, make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), out, stack, A.status, lane);
+            sample_one(X, smp, sidx, make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), out, stack, A.status, lane);
         } else {
-            sample_one(X, smp, D.idx, key, out, stack, A.status, lane);
+            sample_one(X, smp, sidx, key, out, stack, A.status, lane);
         }
         __syncwarp();
     }

@@ -16,6 +16,7 @@ struct SampleArgs {
     uint64_t seed;
     const uint64_t* seeds;  // null, or one seed per batch index: sequence b then samples with key
                             // seeds[b] and sequence index 0, exactly as if it were folded alone
+    const int32_t* stream_idx;   // null, or per batch index: the sequence index of its Philox draws
     const uint8_t* seqs;
     const uint8_t* mask;
     const float* blob32;

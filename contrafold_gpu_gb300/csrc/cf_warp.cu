@@ -140,7 +140,7 @@ __device__ __forceinline__ void fold_one(const WarpArgs& A, const WarpSmemHead* 
         X.T = T;
         const uint64_t sd = A.seeds != nullptr ? A.seeds[D.idx] : A.seed;
         const uint2 key = make_uint2((uint32_t)sd, (uint32_t)(sd >> 32));
-        const int sidx = A.seeds != nullptr ? 0 : D.idx;
+        const int sidx = A.stream_idx != nullptr ? A.stream_idx[D.idx] : (A.seeds != nullptr ? 0 : D.idx);
         for (int smp = 0; smp < A.n_samples; ++smp) {
             char* out = A.out + D.seq_off * (int64_t)A.n_samples + (int64_t)smp * L;
             for (int t = lane; t < L; t += 32) out[t] = '.';

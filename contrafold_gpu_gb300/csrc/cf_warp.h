@@ -31,6 +31,7 @@ struct WarpArgs {
     int n_samples;
     uint64_t seed;
     const uint64_t* seeds;     // null, or per batch index (see SampleArgs::seeds)
+    const int32_t* stream_idx; // null, or per batch index (see SampleArgs::stream_idx)
     char* out;                 // samples at seq_off * n_samples
     int* status;
 };

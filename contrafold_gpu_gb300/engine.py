@@ -28,7 +28,7 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
            "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_engine_load_tuning",
            "cf_engine_tuning_rows", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
-           "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
+           "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_sample_tasks", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group", "cf_plan_set_graph", "cf_plan_schedule", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
            "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats")
@@ -77,6 +77,8 @@ def load_library(path: str = LIB_PATH):
                                 ctypes.c_char_p]
         L.cf_sample_seeded.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, P(ctypes.c_uint64),
                                        ctypes.c_char_p]
+        L.cf_sample_tasks.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
+                                      ctypes.c_char_p]
         L.cf_plan_create.argtypes = [vp, ctypes.c_int32, i64p, ctypes.c_int32, P(vp)]
         L.cf_plan_destroy.argtypes = [vp]
         L.cf_plan_arena_bytes.argtypes = [vp]
@@ -93,7 +95,7 @@ def load_library(path: str = LIB_PATH):
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
                      "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_engine_load_tuning",
                      "cf_engine_tuning_rows", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
-                     "cf_sample_seeded", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
+                     "cf_sample_seeded", "cf_sample_tasks", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group", "cf_plan_set_graph"):
             getattr(L, name).restype = ctypes.c_int
         _lib = L
@@ -180,14 +182,15 @@ class Engine:
         self.mode = mode
 
     def set_schedule(self, kind: str = "auto", ctas_per_sm: int = 0):
-        """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap), 'group' or
-        'cluster' (each sequence folded by a thread-block cluster: latency of long sequences)."""
+        """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap), 'group',
+        'cluster' (each sequence folded by a thread-block cluster: latency of long sequences) or
+        'queue' (one persistent launch, warps pulling (sequence, step, chunk) items)."""
         self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3,
-                                                              "cluster": 4}[kind],
+                                                              "cluster": 4, "queue": 5}[kind],
                                                     int(ctas_per_sm)))
 
     def set_group(self, group: int = 0):
-        """Sequences per CTA of the grouped kernels (0 = automatic)."""
+        """Sequences per CTA of the grouped kernels (<= 32) or of the queue schedule (<= 64); 0 = automatic."""
         self._check(self.lib.cf_engine_set_group(self._h, int(group)))
 
     def set_budget(self, nbytes: int):
@@ -267,6 +270,15 @@ class Engine:
             base = int(B.offsets[b]) * n_samples
             res.append([raw[base + t * L: base + (t + 1) * L] for t in range(n_samples)])
         return res
+
+    def sample_tasks(self, B: Batch, chunk: int = 4096, seed: int = 0) -> List[str]:
+        """One sample per task with the chunk / seed semantics of the
+        reference's fold_tasks_gpu, all tasks in one submission (cf_sample_tasks)."""
+        out = ctypes.create_string_buffer(max(B.total, 1))
+        with self._lock:
+            self._check(self.lib.cf_sample_tasks(*self._args(B), ctypes.c_int32(int(chunk)),
+                                                 ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
+        return B.split_strings(out.raw[:B.total])
 
 
 class Plan:

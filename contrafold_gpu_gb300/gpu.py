@@ -50,8 +50,18 @@ def sample_batch(seqs: Sequence[str], P: dict, n_samples: int, forced_list=None,
 def fold_tasks_gpu(seqs: Sequence[str], forced_masks, P: dict, chunk: int = 4096, seed: int = 0) -> List[str]:
     """One Boltzmann sample per (sequence, mask) task (gpu.py:586-601).
 
-    Tasks are sorted by length and processed in chunks of `chunk`; chunk c0
-    uses seed + c0, as in the reference."""
+    The samples are those of the reference's loop -- tasks sorted by length,
+    chunks of `chunk`, chunk c0 sampled by sample_batch with seed + c0 -- but
+    every task is folded in one device submission (cf_sample_tasks)."""
+    if chunk <= 0:
+        raise ValueError("chunk must be > 0")
+    B = Batch(seqs, _masks(forced_masks, len(seqs)))
+    return engine_for(P).sample_tasks(B, int(chunk), int(seed))
+
+
+def fold_tasks_chunked(seqs: Sequence[str], forced_masks, P: dict, chunk: int = 4096, seed: int = 0) -> List[str]:
+    """The reference's host loop for fold_tasks_gpu (one sample_batch call per
+    chunk of the length-sorted tasks); fold_tasks_gpu returns the same samples."""
     n = len(seqs)
     out: List[Optional[str]] = [None] * n
     order = sorted(range(n), key=lambda k: len(seqs[k]))
