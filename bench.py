@@ -631,9 +631,9 @@ def side_arm(args):
     alpha = np.frombuffer(b"ACGU", np.uint8)
     line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "impl": "ours"}
     if args.workload == "logz":
+        from contrafold_gpu_gb300 import workloads
         n, L = 1000, 128
-        codes = np.random.default_rng(0).integers(0, 4, (n, L))
-        sb = alpha[codes].astype(np.uint8)
+        sb = workloads.logz_128(n, L)
         seqs = [bytes(r).decode() for r in sb]
         offsets = np.arange(n + 1, dtype=np.int64) * L
         d_seqs = torch.from_numpy(sb.reshape(-1).copy()).to(dev)
@@ -691,14 +691,13 @@ def side_arm(args):
                      "clocks": clk.summary()})
         plan.close(); p64.close(); eng.close()
     elif args.workload == "sampling":
+        from contrafold_gpu_gb300 import workloads
         n, S = 4096, 100
-        rng = np.random.default_rng(2)
-        lens = rng.integers(40, 401, n)
-        seqs = [alpha[rng.integers(0, 4, int(L))].tobytes().decode() for L in lens]
+        seqs = workloads.sampling(n)
         B = Batch(seqs)
         res = {}
         with ClockSampler(0) as clk:
-            for sched in ("auto", "warp", "group"):
+            for sched in ("auto", "queue", "warp", "group"):
                 eng = Engine(P)
                 eng.set_schedule(sched)
                 for w in range(args.warmup):
@@ -720,11 +719,9 @@ def side_arm(args):
                      "clocks": clk.summary()})
     else:
         from contrafold_gpu_gb300 import grad
+        from contrafold_gpu_gb300 import workloads
         n, L = 512, 300
-        rng = np.random.default_rng(3)
-        codes = np.random.default_rng(0).integers(0, 4, (n, L))
-        seqs = [bytes(r).decode() for r in alpha[codes].astype(np.uint8)]
-        bonus = rng.normal(0, 0.5, (n, L)).astype(np.float32)
+        seqs, bonus = workloads.grad_300(n, L)
         eng = Engine(P)
         for _ in range(args.warmup):
             grad.logz_grad(seqs, None, list(bonus), engine=eng)
@@ -736,9 +733,14 @@ def side_arm(args):
                 ts.append(time.perf_counter() - t0)
         # sum_k P(k unpaired) + 2 E[#pairs] = L; its float32 residual, relative to L
         ident = float(np.max([abs(res.d_bonus[b].sum() - (L - 2 * res.d_blob[b, 0:25].sum())) for b in range(n)])) / L
+        from contrafold_gpu_gb300.engine import grad_arena_bytes
         line.update({"metric": "logZ gradients/s (708 features + per-position bonus), 512 x 300 nt",
                      "value": n / statistics.mean(ts), "unit": "gradients/s", "higher_is_better": True,
-                     "dtype": "f32 tables, f64 counts", "ms_per_step": 1e3 * statistics.mean(ts),
+                     "dtype": "f32 tables, fixed-point (2^-62) counts", "ms_per_step": 1e3 * statistics.mean(ts),
+                     "memory_per_sequence_bytes": {"300nt_auto": grad_arena_bytes(300, 0),
+                                                   "1000nt_every8": grad_arena_bytes(1000, 8),
+                                                   "1000nt_all": grad_arena_bytes(1000, 1),
+                                                   "3000nt_every8": grad_arena_bytes(3000, 8)},
                      "config": {"workload": "gradient, 512 x 300 nt i.i.d. ACGU, bonuses N(0,0.5) (default_rng(3))",
                                 "api": "grad.logz_grad (host buffers; tying Jacobian on the host)"},
                      "identity_max_rel_err": ident, "clocks": clk.summary()})

@@ -5,6 +5,10 @@ then linked into one shared library that exports the C-ABI of
 include/contrafold_gb300.h.  `-fmad=false` keeps every float add and multiply
 separately rounded (the FP32 paths are bitwise parity targets).
 
+Extra nvcc flags (for example -DCF_FLAT_WALK=0 to compare a kernel variant)
+come from the environment variable CONTRAFOLD_GB300_NVCC_FLAGS; the flags of
+the last build are recorded next to the library, and a change rebuilds it.
+
 `--check` (build(check=True)) builds the same sources with -DCF_CHECK into
 libcontrafold_gb300_check.so: every DP-table subscript of the fold kernels is
 checked against its table's size and reported with printf instead of being
@@ -47,8 +51,22 @@ def _deps():
         [os.path.join(os.path.dirname(HERE), "include", "contrafold_gb300.h")]
 
 
+def _extra_flags():
+    return os.environ.get("CONTRAFOLD_GB300_NVCC_FLAGS", "").split()
+
+
+def _stamp(lib: str) -> str:
+    return lib + ".flags"
+
+
 def up_to_date(lib: str = LIB) -> bool:
     if not os.path.exists(lib):
+        return False
+    try:
+        with open(_stamp(lib)) as fh:
+            if fh.read() != " ".join(_extra_flags()):
+                return False
+    except OSError:
         return False
     t = os.path.getmtime(lib)
     return all(os.path.getmtime(p) <= t for p in _deps())
@@ -65,7 +83,7 @@ def build(force: bool = False, verbose: bool = False, check: bool = False) -> st
     os.makedirs(bdir, exist_ok=True)
     cc = nvcc()
     srcs = _sources()
-    flags = NVCC_FLAGS + (["-DCF_CHECK"] if check else [])
+    flags = NVCC_FLAGS + (["-DCF_CHECK"] if check else []) + _extra_flags()
 
     def compile_one(src):
         obj = os.path.join(bdir, os.path.basename(src).replace(".cu", ".o"))
@@ -87,6 +105,8 @@ def build(force: bool = False, verbose: bool = False, check: bool = False) -> st
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, lib)
+    with open(_stamp(lib), "w") as fh:
+        fh.write(" ".join(_extra_flags()))
     return lib
 
 

@@ -16,8 +16,24 @@
 // derivative of the logZ that cf_logz reports (within float32 rounding).
 //
 // Kernels: one CTA per sequence, threads over the cells of a span (the shape
-// of the plain path); the transition pass runs over all cells at once and
-// accumulates into shared-memory FP64 counters with atomics.
+// of the plain path).  k_adj_inside fills the inside tables; k_adj_outside
+// then walks the diagonals downwards, computing the outside values of
+// diagonal t and, in the same step, the transition probabilities of diagonal
+// t + 1 (whose outside values are final by then).
+//
+// Memory.  The bifurcation and exterior terms read FC, FM, FM1 and the
+// outside FM2o at every span, so those four tables are kept whole.  FCo,
+// FMo and FM1o are read only within 32 diagonals of the one being computed
+// (the single-branch window) and by the counts of their own diagonal, so they
+// live in ring buffers of 33, 2 and 3 diagonals.  The inside FM2 is needed
+// by the counts of its own diagonal only: it is checkpointed on every k-th
+// diagonal and recomputed on the others from FM1 and FM (the same chain in
+// the same order, so bitwise the stored value).  k = 1 keeps every diagonal.
+//
+// Counts are accumulated in 128-bit fixed point (value x 2^62, integer
+// atomics): integer addition is exact and order-independent, so the counts
+// and unpaired probabilities are deterministic -- bitwise the same for every
+// run, thread schedule and checkpoint spacing.
 #include "cf_kernels.h"
 #include "cf_outside.cuh"
 
@@ -26,48 +42,78 @@ namespace {
 
 struct AdjSmem {
     SmemTabs<float> tabs;
+    unsigned long long cnt_lo[CF_BLOB_LEN];   // fixed-point counts (x 2^62), low 64 bits
+    unsigned cnt_hi[CF_BLOB_LEN];             // carries out of cnt_lo (units of 4)
 };
 
-// Adjoint arena: the FP32 arena plus the inside FM2 table, the FP64 prefix of
-// the bonus and the FP64 difference array of the unpaired probabilities.
+// Cells of the FM2 checkpoints (diagonals 0, k, 2k, ... <= L) and the offset
+// of checkpoint c (diagonal c k, m - c k cells).
+__host__ __device__ __forceinline__ int64_t ckpt_off(int c, int m, int k) {
+    return (int64_t)c * m - (int64_t)k * c * (c - 1) / 2;
+}
+__host__ __device__ __forceinline__ int64_t ckpt_cells(int L, int k) { return ckpt_off(L / k + 1, L + 1, k); }
+
+constexpr int kRingFCo = 33;   // FCo: spans t .. t + 32
+constexpr int kRingFMo = 2;    // FMo: spans t, t + 1
+constexpr int kRingFM1o = 3;   // FM1o: spans t .. t + 2
+
+// Adjoint arena (4-byte words): FC FM FM1 (triangles), F5, F5o, FM2o
+// (triangle), the FCo / FMo / FM1o ring buffers, the FM2 checkpoints, the
+// FP64 bonus prefix U, and the fixed-point unpaired difference arrays (adds
+// at lo + 1 and subtractions at hi + 1, 128 bits each: two uint64).
 struct ArenaAdj {
-    Arena32 a;
-    int64_t FM2, U, UD, total;
+    int64_t FC, FM, FM1, F5, F5o, FM2o, RC, RM, R1, FM2, U, UD, total;
 };
-__host__ __device__ __forceinline__ ArenaAdj arena_adj(int L) {
+__host__ __device__ __forceinline__ ArenaAdj arena_adj(int L, int k) {
     ArenaAdj r;
-    r.a = arena32(L);
-    r.FM2 = r.a.total;
-    r.U = r.FM2 + pad32(tri_size(L));               // words; doubles: 2 words each
-    r.UD = r.U + 2 * pad32(L + 2);
-    r.total = r.UD + 2 * pad32(L + 2);
+    const int64_t t = pad32(tri_size(L)), v = pad32(L + 2), rw = pad32(L + 1);
+    r.FC = 0; r.FM = t; r.FM1 = 2 * t; r.F5 = 3 * t; r.F5o = r.F5 + v; r.FM2o = r.F5o + v;
+    r.RC = r.FM2o + t;
+    r.RM = r.RC + kRingFCo * rw;
+    r.R1 = r.RM + kRingFMo * rw;
+    r.FM2 = r.R1 + kRingFM1o * rw;
+    r.U = r.FM2 + pad32(ckpt_cells(L, k));
+    r.UD = r.U + 2 * v;                 // doubles
+    r.total = r.UD + 8 * v;             // 4 x uint64[L + 2]
     return r;
 }
 
+// Outside values of one diagonal live in a ring slot: cell (a, a + t) of
+// table X at X[(t mod R) * rw + a].
 struct AdjView {
     InTabs<float> I;
-    OutTabs O;
-    float* FM2;
-    const double* U;   // U[k] = sum_{t<=k} u_t
-    double* UD;        // unpaired-probability difference array
-    int m;
+    float* F5o;
+    float* FM2o;      // triangle
+    float* RC;        // FCo ring
+    float* RM;        // FMo ring
+    float* R1;        // FM1o ring
+    float* FM2;       // checkpoints
+    const double* U;  // U[k] = sum_{t<=k} u_t
+    unsigned long long* UD;   // [4][L + 2]: add lo, add hi, sub lo, sub hi
+    int m, rw, k, L;
+    __device__ __forceinline__ float& fco(int a, int t) const { return RC[(t % kRingFCo) * rw + a]; }
+    __device__ __forceinline__ float& fmo(int a, int t) const { return RM[(t % kRingFMo) * rw + a]; }
+    __device__ __forceinline__ float& fm1o(int a, int t) const { return R1[(t % kRingFM1o) * rw + a]; }
+    __device__ __forceinline__ float& fm2o(int a, int b) const { return FM2o[tri_off(b - a, m) + a]; }
 };
 
-__device__ __forceinline__ AdjView adj_view(const FoldArgs& A, const SeqDesc& D) {
-    const ArenaAdj r = arena_adj(D.L);
+__device__ __forceinline__ AdjView adj_view(const FoldArgs& A, const SeqDesc& D, int k) {
+    const ArenaAdj r = arena_adj(D.L, k);
     float* base = A.ws + D.ws_off;
     AdjView V;
-    V.I.FC = base + r.a.FC; V.I.FM = base + r.a.FM; V.I.FM1 = base + r.a.FM1; V.I.F5 = base + r.a.F5;
+    V.I.FC = base + r.FC; V.I.FM = base + r.FM; V.I.FM1 = base + r.FM1; V.I.F5 = base + r.F5;
     V.I.m = D.L + 1;
     V.I.sized(D.L);
-    V.O.FC = V.I.FC; V.O.FM = V.I.FM; V.O.FM1 = V.I.FM1; V.O.F5 = V.I.F5;
-    V.O.FCo = base + r.a.FCo; V.O.FMo = base + r.a.FMo; V.O.FM1o = base + r.a.FM1o; V.O.FM2o = base + r.a.FM2o;
-    V.O.F5o = base + r.a.F5o; V.O.m = D.L + 1;
-    V.O.sized(D.L);
+    V.F5o = base + r.F5o;
+    V.FM2o = base + r.FM2o;
+    V.RC = base + r.RC; V.RM = base + r.RM; V.R1 = base + r.R1;
     V.FM2 = base + r.FM2;
     V.U = reinterpret_cast<const double*>(base + r.U);
-    V.UD = reinterpret_cast<double*>(base + r.UD);
+    V.UD = reinterpret_cast<unsigned long long*>(base + r.UD);
     V.m = D.L + 1;
+    V.rw = (int)pad32(D.L + 1);
+    V.k = k;
+    V.L = D.L;
     return V;
 }
 
@@ -102,18 +148,30 @@ __device__ __forceinline__ float single_e(const ParamView<float>& P, const SmemT
     return __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), P.bp(Q.s[p + 1], Q.s[q])), jB1), jB2), snuc);
 }
 
+
+// FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j], k ascending, live terms only.
+__device__ __forceinline__ float fm2_chain(const LseAcc32& sr, const InTabs<float>& T, int i, int j) {
+    float fm2 = CF_NEG32;
+    for (int k = i + 1; k < j; ++k) {
+        const float a = T.FM1[T.at(i, k)], b = T.FM[T.at(k, j)];
+        if (a > CF_HALF32 && b > CF_HALF32) fm2 = sr.plus(fm2, __fadd_rn(a, b));
+    }
+    return fm2;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Inside with bonus (accurate float32 log-sum-exp)
+// Inside with bonus (accurate float32 log-sum-exp); FM2 kept on every ckpt-th
+// diagonal.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const float* bonus) {
+__global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const float* bonus, int ckpt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<AdjSmem*>(smem_raw);
     SeqDesc D;
     const SeqView Q = adj_setup(sm, A, D);
     const ParamView<float> P{sm->tabs.blob};
-    const AdjView V = adj_view(A, D);
+    const AdjView V = adj_view(A, D, ckpt);
     const LseAcc32 sr{};
     const int L = D.L, m = L + 1;
     double* U = const_cast<double*>(V.U);
@@ -129,17 +187,14 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const f
     __syncthreads();
     const InTabs<float>& T = V.I;
     for (int d = 0; d <= L; ++d) {
+        const bool keep = d % ckpt == 0;
+        float* fm2_ck = V.FM2 + (keep ? ckpt_off(d / ckpt, m, ckpt) : 0);
         for (int i = threadIdx.x; i + d <= L; i += blockDim.x) {
             const int j = i + d, at = tri_off(d, m) + i;
             const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
             const bool fc_cell = (0 < i) && (j < L) && Q.pairable(i, j + 1);
-            float fm2 = CF_NEG32;
-            if (fm_region)
-                for (int k = i + 1; k < j; ++k) {
-                    const float a = T.FM1[T.at(i, k)], b = T.FM[T.at(k, j)];
-                    if (a > CF_HALF32 && b > CF_HALF32) fm2 = sr.plus(fm2, __fadd_rn(a, b));
-                }
-            V.FM2[at] = fm2;
+            const float fm2 = fm_region ? fm2_chain(sr, T, i, j) : CF_NEG32;
+            if (keep) fm2_ck[i] = fm2;
             float fc = CF_NEG32;
             if (fc_cell) {
                 const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
@@ -222,21 +277,245 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const f
 }
 
 // ---------------------------------------------------------------------------
-// Outside with bonus (gathers; any order -- no bitwise target)
+// Outside with bonus (gathers; any order -- no bitwise target) and, one
+// diagonal behind, the transition probabilities -> fixed-point expected counts
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const float* bonus) {
+namespace {
+
+// Fixed point: a probability v (float, < 4) as the integer v x 2^62 (exact:
+// a float has 24 significant bits).  A 128-bit sum of such integers is exact
+// in any order.
+__device__ __forceinline__ unsigned long long fixp(float v) { return __float2ull_rn(ldexpf(v, 62)); }
+
+__device__ __forceinline__ void add128(unsigned long long* lo, unsigned* hi, unsigned long long x) {
+    const unsigned long long old = atomicAdd(lo, x);
+    if (old + x < old) atomicAdd(hi, 1u);
+}
+__device__ __forceinline__ void add128g(unsigned long long* lo, unsigned long long* hi, unsigned long long x) {
+    const unsigned long long old = atomicAdd(lo, x);
+    if (old + x < old) atomicAdd(hi, 1ull);
+}
+
+struct Counter {
+    AdjSmem* sm;
+    unsigned long long* ud;   // global [4][L + 2]: add lo, add hi, sub lo, sub hi
+    int n;                    // L + 2
+    __device__ __forceinline__ void add(int e, unsigned long long v) const { add128(&sm->cnt_lo[e], &sm->cnt_hi[e], v); }
+    // positions (lo, hi] unpaired with probability v
+    __device__ __forceinline__ void unp(int lo, int hi, unsigned long long v) const {
+        if (hi <= lo) return;
+        add128g(ud + lo + 1, ud + n + lo + 1, v);
+        add128g(ud + 2 * n + hi + 1, ud + 3 * n + hi + 1, v);
+    }
+};
+
+// jA(i, j) of the pair (i, j+1): entries hc[s_i][s_j+1], dl (i < L), dr (j > 0)
+__device__ __forceinline__ void count_jA(const Counter& C, const SeqView& Q, int L, int i, int j, unsigned long long v) {
+    C.add(CF_OFF_HC + Q.s[i] * 5 + Q.s[j + 1], v);
+    if (i < L) C.add(CF_OFF_DL + (Q.s[i] * 5 + Q.s[j + 1]) * 5 + Q.s[i + 1], v);
+    if (j > 0) C.add(CF_OFF_DR + (Q.s[i] * 5 + Q.s[j + 1]) * 5 + Q.s[j], v);
+}
+// jA(j, i) of the pair (i+1, j)
+__device__ __forceinline__ void count_jA_rev(const Counter& C, const SeqView& Q, int L, int i, int j,
+                                             unsigned long long v) {
+    C.add(CF_OFF_HC + Q.s[j] * 5 + Q.s[i + 1], v);
+    if (j < L) C.add(CF_OFF_DL + (Q.s[j] * 5 + Q.s[i + 1]) * 5 + Q.s[j + 1], v);
+    if (i > 0) C.add(CF_OFF_DR + (Q.s[j] * 5 + Q.s[i + 1]) * 5 + Q.s[i], v);
+}
+// jB = hc + tm of the pair (a, b+1) with inner neighbours (a+1, b)
+__device__ __forceinline__ void count_jB(const Counter& C, int sa, int sb1, int sa1, int sb, unsigned long long v) {
+    C.add(CF_OFF_HC + sa * 5 + sb1, v);
+    C.add(CF_OFF_TM + idx4(sa, sb1, sa1, sb), v);
+}
+
+// Outside values of cell (a, b), span t, into the ring slots of diagonal t.
+__device__ __forceinline__ void outside_cell(const AdjSmem* sm, const ParamView<float>& P, const SeqView& Q,
+                                             const AdjView& V, int a, int b) {
+    const LseAcc32 sr{};
+    const int L = V.L, t = b - a;
+    const InTabs<float>& I = V.I;
+    const bool fm_region = (0 < a) && (a + 2 <= b) && (b < L);
+    float fmo = CF_NEG32, fm1o = CF_NEG32;
+    if (fm_region) {
+        float acc = CF_NEG32;
+        for (int i = 1; i < a; ++i) {
+            const float src = V.fm2o(i, b), f1 = I.FM1[I.at(i, a)];
+            if (src > CF_HALF32 && f1 > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, f1));
+        }
+        if (b + 1 < L) acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.fmo(a, t + 1), P.mu()), ubon(V.U, b + 1)));
+        fmo = acc;
+        acc = CF_NEG32;
+        if (a >= 2) acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.fm1o(a - 1, t + 1), P.mu()), ubon(V.U, a)));
+        for (int j = b + 1; j < L; ++j) {
+            const float src = V.fm2o(a, j), fmk = I.FM[I.at(b, j)];
+            if (src > CF_HALF32 && fmk > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, fmk));
+        }
+        fm1o = sr.plus(acc, fmo);
+    }
+    V.fmo(a, t) = fmo;
+    V.fm1o(a, t) = fm1o;
+    float fco = CF_NEG32;
+    if (0 < a && b < L && Q.pairable(a, b + 1)) {
+        const int sa = Q.s[a], sb1 = Q.s[b + 1];
+        float acc = CF_NEG32;
+        const float f5k = I.F5[a - 1];
+        if (f5k > CF_HALF32) {
+            const float jA = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
+            acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V.F5o[b + 1], P.ep()), P.bp(sa, sb1)), jA), f5k));
+        }
+        if (a >= 2 && b + 1 < L) {
+            const float jAji = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
+            acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(V.fm1o(a - 1, t + 2), jAji), P.mp()), P.bp(sa, sb1)));
+        }
+        for (int l1 = 0; l1 <= CMAX; ++l1) {
+            const int i = a - 1 - l1;
+            if (i < 1) break;
+            for (int l2 = 0; l1 + l2 <= CMAX; ++l2) {
+                const int j = b + 1 + l2;
+                if (j >= L) break;
+                if (!Q.pairable(i, j + 1)) continue;
+                const float src = V.fco(i, j - i);
+                if (!(src > CF_HALF32)) continue;
+                const float e = single_e(P, &sm->tabs, Q, i, j, a - 1, b + 1);
+                const float bb = __fadd_rn(bon(V.U, i, a - 1), bon(V.U, b + 1, j));
+                acc = sr.plus(acc, __fadd_rn(__fadd_rn(src, e), bb));
+            }
+        }
+        fco = acc;
+    }
+    V.fco(a, t) = fco;
+    float fm2o = CF_NEG32;
+    if (fm_region) fm2o = sr.plus(fm2o, fmo);
+    if (fco > CF_HALF32) {
+        const float jA = junctionA<LseAcc32>(P, L, Q, a, b);
+        fm2o = sr.plus(fm2o, __fadd_rn(__fadd_rn(__fadd_rn(fco, jA), P.mp()), P.mb()));
+    }
+    V.fm2o(a, b) = fm2o;
+}
+
+// Transitions out of the states of cell (i, j) (its outside values final).
+__device__ __forceinline__ void count_cell(const AdjSmem* sm, const ParamView<float>& P, const SeqView& Q,
+                                           const AdjView& V, const Counter& C, float Z, int i, int j) {
+    const LseAcc32 sr{};
+    const int L = V.L, d = j - i, m = V.m;
+    const InTabs<float>& I = V.I;
+    auto prob = [&](float x) { return fixp(expf(__fsub_rn(x, Z))); };
+    const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
+    if (0 < i && j < L && Q.pairable(i, j + 1)) {
+        const float fco = V.fco(i, d);
+        if (fco > CF_HALF32) {
+            const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
+            const float jB = sm->tabs.jB[idx4(si, sj1, si1, sj)];
+            // hairpin
+            {
+                const int hl = d <= DHP ? d : DHP;
+                const unsigned long long v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(jB, P.hp(hl)), bon(V.U, i, j))));
+                count_jB(C, si, sj1, si1, sj, v);
+                C.add(CF_OFF_HPCUM + hl, v);
+                C.unp(i, j, v);
+            }
+            // single-branch loops
+            unsigned long long outer_jB = 0;
+            const int pmax = (i + CMAX < j) ? i + CMAX : j;
+            for (int p = i; p <= pmax; ++p) {
+                int qmin = p + 2;
+                if (p - i + j - CMAX > qmin) qmin = p - i + j - CMAX;
+                for (int q = j; q >= qmin; --q) {
+                    if (!Q.pairable(p + 1, q)) continue;
+                    const float inner = I.FC[I.at(p + 1, q - 1)];
+                    if (!(inner > CF_HALF32)) continue;
+                    const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
+                    const float bb = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
+                    const unsigned long long v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(e, inner), bb)));
+                    const int l1 = p - i, l2 = j - q;
+                    if (l1 == 0 && l2 == 0) {
+                        C.add(CF_OFF_BP + si1 * 5 + sj, v);
+                        C.add(CF_OFF_STACK + idx4(si, sj1, si1, sj), v);
+                    } else {
+                        const int sa = Q.s[p + 1], sq = Q.s[q];
+                        C.add(CF_OFF_CS + l1 * 31 + l2, v);
+                        C.add(CF_OFF_BP + sa * 5 + sq, v);
+                        outer_jB += v;
+                        count_jB(C, sq, sa, Q.s[q + 1], Q.s[p], v);
+                        if (l1 == 0 && l2 == 1) C.add(CF_OFF_B01 + sj, v);
+                        else if (l1 == 1 && l2 == 0) C.add(CF_OFF_B01 + si1, v);
+                        else if (l1 == 1 && l2 == 1) C.add(CF_OFF_I11 + si1 * 5 + sj, v);
+                    }
+                    C.unp(i, p, v);
+                    C.unp(q, j, v);
+                }
+            }
+            if (outer_jB != 0) count_jB(C, si, sj1, si1, sj, outer_jB);
+            // multiloop closed by (i, j+1): FM2 from its checkpoint, or recomputed
+            if (fm_region) {
+                const float fm2 = d % V.k == 0 ? V.FM2[ckpt_off(d / V.k, m, V.k) + i] : fm2_chain(sr, I, i, j);
+                if (fm2 > CF_HALF32) {
+                    const float jA = junctionA<LseAcc32>(P, L, Q, i, j);
+                    const unsigned long long v =
+                        prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(__fadd_rn(fm2, jA), P.mp()), P.mb())));
+                    count_jA(C, Q, L, i, j, v);
+                    C.add(CF_OFF_MP, v);
+                    C.add(CF_OFF_MB, v);
+                }
+            }
+        }
+    }
+    if (fm_region) {
+        const float fm1o = V.fm1o(i, d);
+        if (fm1o > CF_HALF32) {
+            const float fin = I.FC[I.at(i + 1, j - 1)];
+            if (Q.pairable(i + 1, j) && fin > CF_HALF32) {
+                const float jAji = junctionA_rev<LseAcc32>(P, L, Q, i, j);
+                const unsigned long long v = prob(__fadd_rn(fm1o, __fadd_rn(__fadd_rn(__fadd_rn(fin, jAji), P.mp()),
+                                                                             P.bp(Q.s[i + 1], Q.s[j]))));
+                count_jA_rev(C, Q, L, i, j, v);
+                C.add(CF_OFF_MP, v);
+                C.add(CF_OFF_BP + Q.s[i + 1] * 5 + Q.s[j], v);
+            }
+            const float ext = I.FM1[I.at(i + 1, j)];
+            if (ext > CF_HALF32) {
+                const unsigned long long v = prob(__fadd_rn(fm1o, __fadd_rn(__fadd_rn(ext, P.mu()), ubon(V.U, i + 1))));
+                C.add(CF_OFF_MU, v);
+                C.unp(i, i + 1, v);
+            }
+        }
+        const float fmo = V.fmo(i, d);
+        const float prev = I.FM[I.at(i, j - 1)];
+        if (fmo > CF_HALF32 && prev > CF_HALF32) {
+            const unsigned long long v = prob(__fadd_rn(fmo, __fadd_rn(__fadd_rn(prev, P.mu()), ubon(V.U, j))));
+            C.add(CF_OFF_MU, v);
+            C.unp(j - 1, j, v);
+        }
+    }
+}
+
+// 128-bit fixed point (hi: units of 2^64, lo) -> double
+__device__ __forceinline__ double fixp_value(double hi, unsigned long long lo) {
+    return hi * 4.0 + (double)(lo >> 10) * 0x1p-52 + (double)(lo & 1023ull) * 0x1p-62;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const float* bonus, int ckpt,
+                                                               double* counts_out, double* unpaired_out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<AdjSmem*>(smem_raw);
     SeqDesc D;
     const SeqView Q = adj_setup(sm, A, D);
     const ParamView<float> P{sm->tabs.blob};
-    const AdjView V = adj_view(A, D);
+    const AdjView V = adj_view(A, D, ckpt);
     const LseAcc32 sr{};
-    const int L = D.L, m = L + 1;
-    const OutTabs& T = V.O;
+    const int L = D.L;
+    const InTabs<float>& I = V.I;
+    for (int e = threadIdx.x; e < CF_BLOB_LEN; e += blockDim.x) {
+        sm->cnt_lo[e] = 0ull;
+        sm->cnt_hi[e] = 0u;
+    }
+    for (int k = threadIdx.x; k < 4 * (L + 2); k += blockDim.x) V.UD[k] = 0ull;
+    // exterior outside F5o (one warp)
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
-        if (lane == 0) T.F5o[L] = 0.0f;
+        if (lane == 0) V.F5o[L] = 0.0f;
         __syncwarp();
         for (int k = L - 1; k >= 0; --k) {
             float acc = CF_NEG32;
@@ -245,10 +524,10 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
                 bool ok = false;
                 float term = 0.0f;
                 if (j >= k + 2 && Q.pairable(k + 1, j)) {
-                    const float fcin = T.FC[T.at(k + 1, j - 1)];
+                    const float fcin = I.FC[I.at(k + 1, j - 1)];
                     if (fcin > CF_HALF32) {
                         const float jA = junctionA_rev<LseAcc32>(P, L, Q, k, j);
-                        term = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(T.F5o[j], P.ep()), P.bp(Q.s[k + 1], Q.s[j])), jA), fcin);
+                        term = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V.F5o[j], P.ep()), P.bp(Q.s[k + 1], Q.s[j])), jA), fcin);
                         ok = true;
                     }
                 }
@@ -259,233 +538,31 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
                     acc = sr.plus(acc, __shfl_sync(0xffffffffu, term, t));
                 }
             }
-            acc = sr.plus(acc, __fadd_rn(__fadd_rn(T.F5o[k + 1], P.eu()), ubon(V.U, k + 1)));
-            if (lane == 0) T.F5o[k] = acc;
+            acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.F5o[k + 1], P.eu()), ubon(V.U, k + 1)));
+            if (lane == 0) V.F5o[k] = acc;
             __syncwarp();
         }
     }
     __syncthreads();
-    for (int d = L; d >= 0; --d) {
-        for (int a = threadIdx.x; a + d <= L; a += blockDim.x) {
-            const int b = a + d, at = tri_off(d, m) + a;
-            const bool fm_region = (0 < a) && (a + 2 <= b) && (b < L);
-            float fmo = CF_NEG32, fm1o = CF_NEG32;
-            if (fm_region) {
-                float acc = CF_NEG32;
-                for (int i = 1; i < a; ++i) {
-                    const float src = T.FM2o[T.at(i, b)], f1 = T.FM1[T.at(i, a)];
-                    if (src > CF_HALF32 && f1 > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, f1));
-                }
-                if (b + 1 < L) acc = sr.plus(acc, __fadd_rn(__fadd_rn(T.FMo[T.at(a, b + 1)], P.mu()), ubon(V.U, b + 1)));
-                fmo = acc;
-                acc = CF_NEG32;
-                if (a >= 2) acc = sr.plus(acc, __fadd_rn(__fadd_rn(T.FM1o[T.at(a - 1, b)], P.mu()), ubon(V.U, a)));
-                for (int j = b + 1; j < L; ++j) {
-                    const float src = T.FM2o[T.at(a, j)], fmk = T.FM[T.at(b, j)];
-                    if (src > CF_HALF32 && fmk > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, fmk));
-                }
-                fm1o = sr.plus(acc, fmo);
-            }
-            T.FMo[at] = fmo;
-            T.FM1o[at] = fm1o;
-            float fco = CF_NEG32;
-            if (0 < a && b < L && Q.pairable(a, b + 1)) {
-                const int sa = Q.s[a], sb1 = Q.s[b + 1];
-                float acc = CF_NEG32;
-                const float f5k = T.F5[a - 1];
-                if (f5k > CF_HALF32) {
-                    const float jA = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
-                    acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(T.F5o[b + 1], P.ep()), P.bp(sa, sb1)), jA), f5k));
-                }
-                if (a >= 2 && b + 1 < L) {
-                    const float jAji = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
-                    acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(T.FM1o[T.at(a - 1, b + 1)], jAji), P.mp()), P.bp(sa, sb1)));
-                }
-                for (int l1 = 0; l1 <= CMAX; ++l1) {
-                    const int i = a - 1 - l1;
-                    if (i < 1) break;
-                    for (int l2 = 0; l1 + l2 <= CMAX; ++l2) {
-                        const int j = b + 1 + l2;
-                        if (j >= L) break;
-                        if (!Q.pairable(i, j + 1)) continue;
-                        const float src = T.FCo[T.at(i, j)];
-                        if (!(src > CF_HALF32)) continue;
-                        const float e = single_e(P, &sm->tabs, Q, i, j, a - 1, b + 1);
-                        const float bb = __fadd_rn(bon(V.U, i, a - 1), bon(V.U, b + 1, j));
-                        acc = sr.plus(acc, __fadd_rn(__fadd_rn(src, e), bb));
-                    }
-                }
-                fco = acc;
-            }
-            T.FCo[at] = fco;
-            float fm2o = CF_NEG32;
-            if (fm_region) fm2o = sr.plus(fm2o, fmo);
-            if (fco > CF_HALF32) {
-                const float jA = junctionA<LseAcc32>(P, L, Q, a, b);
-                fm2o = sr.plus(fm2o, __fadd_rn(__fadd_rn(__fadd_rn(fco, jA), P.mp()), P.mb()));
-            }
-            T.FM2o[at] = fm2o;
+    const Counter C{sm, V.UD, L + 2};
+    const float Z = I.F5[L];
+    // step t: outside values of diagonal t, counts of diagonal t + 1 (final since the last step)
+    for (int t = L; t >= -1; --t) {
+        const int no = t >= 0 ? L + 1 - t : 0;
+        const int nc = t + 1 <= L ? L - t : 0;
+        for (int c = threadIdx.x; c < no + nc; c += blockDim.x) {
+            if (c < no) outside_cell(sm, P, Q, V, c, c + t);
+            else count_cell(sm, P, Q, V, C, Z, c - no, c - no + t + 1);
         }
         __syncthreads();
     }
-}
-
-// ---------------------------------------------------------------------------
-// Transition probabilities -> FP64 expected counts
-// ---------------------------------------------------------------------------
-namespace {
-
-struct Counter {
-    double* c;    // shared [CF_BLOB_LEN]
-    double* ud;   // global unpaired difference array [L + 2]
-    __device__ __forceinline__ void add(int e, double v) const { atomicAdd(c + e, v); }
-    // positions (lo, hi] unpaired with probability v
-    __device__ __forceinline__ void unp(int lo, int hi, double v) const {
-        if (hi <= lo) return;
-        atomicAdd(ud + lo + 1, v);
-        atomicAdd(ud + hi + 1, -v);
-    }
-};
-
-// jA(i, j) of the pair (i, j+1): entries hc[s_i][s_j+1], dl (i < L), dr (j > 0)
-__device__ __forceinline__ void count_jA(const Counter& C, const SeqView& Q, int L, int i, int j, double v) {
-    C.add(CF_OFF_HC + Q.s[i] * 5 + Q.s[j + 1], v);
-    if (i < L) C.add(CF_OFF_DL + (Q.s[i] * 5 + Q.s[j + 1]) * 5 + Q.s[i + 1], v);
-    if (j > 0) C.add(CF_OFF_DR + (Q.s[i] * 5 + Q.s[j + 1]) * 5 + Q.s[j], v);
-}
-// jA(j, i) of the pair (i+1, j)
-__device__ __forceinline__ void count_jA_rev(const Counter& C, const SeqView& Q, int L, int i, int j, double v) {
-    C.add(CF_OFF_HC + Q.s[j] * 5 + Q.s[i + 1], v);
-    if (j < L) C.add(CF_OFF_DL + (Q.s[j] * 5 + Q.s[i + 1]) * 5 + Q.s[j + 1], v);
-    if (i > 0) C.add(CF_OFF_DR + (Q.s[j] * 5 + Q.s[i + 1]) * 5 + Q.s[i], v);
-}
-// jB = hc + tm of the pair (a, b+1) with inner neighbours (a+1, b)
-__device__ __forceinline__ void count_jB(const Counter& C, int sa, int sb1, int sa1, int sb, double v) {
-    C.add(CF_OFF_HC + sa * 5 + sb1, v);
-    C.add(CF_OFF_TM + idx4(sa, sb1, sa1, sb), v);
-}
-
-}  // namespace
-
-__global__ void __launch_bounds__(kFoldThreads) k_adj_counts(FoldArgs A, const float* bonus, double* counts_out,
-                                                              double* unpaired_out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto* sm = reinterpret_cast<AdjSmem*>(smem_raw);
-    __shared__ double cnt[CF_BLOB_LEN];
-    SeqDesc D;
-    const SeqView Q = adj_setup(sm, A, D);
-    const ParamView<float> P{sm->tabs.blob};
-    const AdjView V = adj_view(A, D);
-    const int L = D.L, m = L + 1;
-    for (int e = threadIdx.x; e < CF_BLOB_LEN; e += blockDim.x) cnt[e] = 0.0;
-    for (int k = threadIdx.x; k < L + 2; k += blockDim.x) V.UD[k] = 0.0;
-    __syncthreads();
-    const Counter C{cnt, V.UD};
-    const InTabs<float>& I = V.I;
-    const OutTabs& O = V.O;
-    const float Z = I.F5[L];
-    auto prob = [&](float x) -> double { return (double)expf(__fsub_rn(x, Z)); };
-    const int ncell = (int)tri_size(L);
-    // cells (i, j) in diagonal-major order, all independent
-    int i = threadIdx.x;
-    for (int d = 0; d <= L; ++d) {
-        const int cntd = m - d;
-        for (; i < cntd; i += blockDim.x) {
-            const int j = i + d;
-            const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
-            if (0 < i && j < L && Q.pairable(i, j + 1)) {
-                const float fco = O.FCo[tri_off(d, m) + i];
-                if (fco > CF_HALF32) {
-                    const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
-                    const float jB = sm->tabs.jB[idx4(si, sj1, si1, sj)];
-                    // hairpin
-                    {
-                        const int hl = d <= DHP ? d : DHP;
-                        const double v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(jB, P.hp(hl)), bon(V.U, i, j))));
-                        count_jB(C, si, sj1, si1, sj, v);
-                        C.add(CF_OFF_HPCUM + hl, v);
-                        C.unp(i, j, v);
-                    }
-                    // single-branch loops
-                    double outer_jB = 0.0;
-                    const int pmax = (i + CMAX < j) ? i + CMAX : j;
-                    for (int p = i; p <= pmax; ++p) {
-                        int qmin = p + 2;
-                        if (p - i + j - CMAX > qmin) qmin = p - i + j - CMAX;
-                        for (int q = j; q >= qmin; --q) {
-                            if (!Q.pairable(p + 1, q)) continue;
-                            const float inner = I.FC[I.at(p + 1, q - 1)];
-                            if (!(inner > CF_HALF32)) continue;
-                            const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
-                            const float bb = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
-                            const double v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(e, inner), bb)));
-                            const int l1 = p - i, l2 = j - q;
-                            if (l1 == 0 && l2 == 0) {
-                                C.add(CF_OFF_BP + si1 * 5 + sj, v);
-                                C.add(CF_OFF_STACK + idx4(si, sj1, si1, sj), v);
-                            } else {
-                                const int sa = Q.s[p + 1], sq = Q.s[q];
-                                C.add(CF_OFF_CS + l1 * 31 + l2, v);
-                                C.add(CF_OFF_BP + sa * 5 + sq, v);
-                                outer_jB += v;
-                                count_jB(C, sq, sa, Q.s[q + 1], Q.s[p], v);
-                                if (l1 == 0 && l2 == 1) C.add(CF_OFF_B01 + sj, v);
-                                else if (l1 == 1 && l2 == 0) C.add(CF_OFF_B01 + si1, v);
-                                else if (l1 == 1 && l2 == 1) C.add(CF_OFF_I11 + si1 * 5 + sj, v);
-                            }
-                            C.unp(i, p, v);
-                            C.unp(q, j, v);
-                        }
-                    }
-                    if (outer_jB != 0.0) count_jB(C, si, sj1, si1, sj, outer_jB);
-                    // multiloop closed by (i, j+1)
-                    const float fm2 = V.FM2[tri_off(d, m) + i];
-                    if (fm2 > CF_HALF32) {
-                        const float jA = junctionA<LseAcc32>(P, L, Q, i, j);
-                        const double v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(__fadd_rn(fm2, jA), P.mp()), P.mb())));
-                        count_jA(C, Q, L, i, j, v);
-                        C.add(CF_OFF_MP, v);
-                        C.add(CF_OFF_MB, v);
-                    }
-                }
-            }
-            if (fm_region) {
-                const float fm1o = O.FM1o[tri_off(d, m) + i];
-                if (fm1o > CF_HALF32) {
-                    const float fin = I.FC[I.at(i + 1, j - 1)];
-                    if (Q.pairable(i + 1, j) && fin > CF_HALF32) {
-                        const float jAji = junctionA_rev<LseAcc32>(P, L, Q, i, j);
-                        const double v = prob(__fadd_rn(fm1o, __fadd_rn(__fadd_rn(__fadd_rn(fin, jAji), P.mp()),
-                                                                           P.bp(Q.s[i + 1], Q.s[j]))));
-                        count_jA_rev(C, Q, L, i, j, v);
-                        C.add(CF_OFF_MP, v);
-                        C.add(CF_OFF_BP + Q.s[i + 1] * 5 + Q.s[j], v);
-                    }
-                    const float ext = I.FM1[I.at(i + 1, j)];
-                    if (ext > CF_HALF32) {
-                        const double v = prob(__fadd_rn(fm1o, __fadd_rn(__fadd_rn(ext, P.mu()), ubon(V.U, i + 1))));
-                        C.add(CF_OFF_MU, v);
-                        C.unp(i, i + 1, v);
-                    }
-                }
-                const float fmo = O.FMo[tri_off(d, m) + i];
-                const float prev = I.FM[I.at(i, j - 1)];
-                if (fmo > CF_HALF32 && prev > CF_HALF32) {
-                    const double v = prob(__fadd_rn(fmo, __fadd_rn(__fadd_rn(prev, P.mu()), ubon(V.U, j))));
-                    C.add(CF_OFF_MU, v);
-                    C.unp(j - 1, j, v);
-                }
-            }
-        }
-        i -= cntd;
-    }
-    (void)ncell;
     // exterior transitions: threads over j
     for (int j = 1 + threadIdx.x; j <= L; j += blockDim.x) {
-        const float f5o = O.F5o[j];
+        const float f5o = V.F5o[j];
         if (!(f5o > CF_HALF32)) continue;
         {
-            const double v = prob(__fadd_rn(f5o, __fadd_rn(__fadd_rn(I.F5[j - 1], P.eu()), ubon(V.U, j))));
+            const unsigned long long v =
+                fixp(expf(__fsub_rn(__fadd_rn(f5o, __fadd_rn(__fadd_rn(I.F5[j - 1], P.eu()), ubon(V.U, j))), Z)));
             C.add(CF_OFF_EU, v);
             C.unp(j - 1, j, v);
         }
@@ -494,8 +571,9 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_counts(FoldArgs A, const f
             const float fcin = I.FC[I.at(k + 1, j - 1)], f5k = I.F5[k];
             if (!(fcin > CF_HALF32) || !(f5k > CF_HALF32)) continue;
             const float jA = junctionA_rev<LseAcc32>(P, L, Q, k, j);
-            const double v = prob(__fadd_rn(f5o, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(f5k, fcin), P.ep()),
-                                                                      P.bp(Q.s[k + 1], Q.s[j])), jA)));
+            const unsigned long long v = fixp(expf(__fsub_rn(
+                __fadd_rn(f5o, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(f5k, fcin), P.ep()), P.bp(Q.s[k + 1], Q.s[j])), jA)),
+                Z)));
             count_jA_rev(C, Q, L, k, j, v);
             C.add(CF_OFF_EP, v);
             C.add(CF_OFF_BP + Q.s[k + 1] * 5 + Q.s[j], v);
@@ -503,18 +581,28 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_counts(FoldArgs A, const f
     }
     __syncthreads();
     double* out = counts_out + (int64_t)D.idx * CF_BLOB_LEN;
-    for (int e = threadIdx.x; e < CF_BLOB_LEN; e += blockDim.x) out[e] = cnt[e];
+    for (int e = threadIdx.x; e < CF_BLOB_LEN; e += blockDim.x) out[e] = fixp_value((double)sm->cnt_hi[e], sm->cnt_lo[e]);
     if (threadIdx.x == 0) {
-        double acc = 0.0;
+        // running 128-bit prefix of (adds - subtractions): P(k unpaired), exact, then rounded once
+        const int n = L + 2;
+        unsigned long long lo = 0ull;
+        long long hi = 0;
         for (int k = 1; k <= L; ++k) {
-            acc += V.UD[k];
-            unpaired_out[D.seq_off + k - 1] = acc;
+            const unsigned long long al = V.UD[k], sl = V.UD[2 * n + k];
+            const long long ah = (long long)V.UD[n + k], sh = (long long)V.UD[3 * n + k];
+            const unsigned long long lo1 = lo + al;
+            hi += ah + (lo1 < lo ? 1 : 0);
+            const unsigned long long lo2 = lo1 - sl;
+            hi -= sh + (lo2 > lo1 ? 1 : 0);
+            lo = lo2;
+            unpaired_out[D.seq_off + k - 1] = fixp_value((double)hi, lo);
         }
         if (A.logz) A.logz[D.idx] = Z;
     }
 }
 
 size_t adj_smem_bytes(int Lmax) { return sizeof(AdjSmem) + 2 * (size_t)((Lmax + 2 + 15) & ~15); }
-int64_t adj_arena_words(int L) { return arena_adj(L).total; }
+int64_t adj_arena_words(int L, int ckpt) { return arena_adj(L, ckpt).total; }
+int adj_auto_checkpoint(int L) { return L < 512 ? 1 : 8; }
 
 }  // namespace cf

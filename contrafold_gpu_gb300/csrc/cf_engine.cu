@@ -78,13 +78,13 @@ struct DevBuf {
 
 enum Job { JOB_LOGZ = 0, JOB_LOGZ64, JOB_BPP, JOB_MEA, JOB_MFE, JOB_SAMPLE, JOB_GRAD };
 
-int64_t arena_words(Job job, int L) {
+int64_t arena_words(Job job, int L, int grad_ckpt = 1) {
     switch (job) {
         case JOB_LOGZ:
         case JOB_SAMPLE: return cf::pad32(cf::arena32_inside_words(L));
         case JOB_LOGZ64:
         case JOB_MFE: return cf::arena64(L).total;
-        case JOB_GRAD: return cf::pad32(cf::adj_arena_words(L));
+        case JOB_GRAD: return cf::pad32(cf::adj_arena_words(L, grad_ckpt));
         default: return cf::arena32(L).total;
     }
 }
@@ -223,6 +223,7 @@ struct cf_engine {
     int group = 0;       // sequences per CTA of the grouped kernels (0 = auto)
     size_t smem_optin = 0;
     std::vector<TuneRow> tuning = default_tuning();   // schedule table of the automatic path
+    int grad_ckpt = 0;   // FM2 checkpoint spacing of cf_grad (0 = automatic by the longest sequence)
 };
 
 namespace {
@@ -248,6 +249,7 @@ struct Plan {
     int wgrid = 0;                // its grid
     int64_t slot_words = 0;       // its arena slot per warp
     std::vector<SeqDesc> descs;   // grouped order
+    int grad_ckpt = 1;            // cf_grad: FM2 kept on every grad_ckpt-th diagonal
     std::vector<int> slice_begin; // descs index where each arena slice starts (group aligned)
     std::vector<int64_t> slice_words;
     int group = 1;
@@ -413,6 +415,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         }
         P.warp = false;   // not even one CTA of warp slots fits: per-sequence kernels, sliced
     }
+    P.grad_ckpt = eng->grad_ckpt > 0 ? eng->grad_ckpt : cf::adj_auto_checkpoint(P.Lmax);
     P.slice_begin.clear();
     P.slice_words.clear();
     int64_t cur = 0;
@@ -420,7 +423,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
     for (int k = 0; k < n; k += P.group) {
         int64_t gw = 0;
         const int kend = std::min(n, k + P.group);
-        for (int t = k; t < kend; ++t) gw += arena_words(job, P.descs[t].L);
+        for (int t = k; t < kend; ++t) gw += arena_words(job, P.descs[t].L, P.grad_ckpt);
         if (gw > budget_words) return fail(CF_ENOMEM, "sequence group does not fit the arena budget");
         if (cur + gw > budget_words && k > start) {
             P.slice_begin.push_back(start);
@@ -430,7 +433,7 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         }
         for (int t = k; t < kend; ++t) {
             P.descs[t].ws_off = cur;
-            cur += arena_words(job, P.descs[t].L);
+            cur += arena_words(job, P.descs[t].L, P.grad_ckpt);
         }
     }
     P.slice_begin.push_back(start);
@@ -983,6 +986,19 @@ int cf_engine_load_tuning(cf_engine* e, const char* path) {
 
 int cf_engine_tuning_rows(const cf_engine* e) { return e ? (int)e->tuning.size() : 0; }
 
+int cf_engine_set_grad_checkpoint(cf_engine* e, int32_t every) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    if (every < 0) return fail(CF_EINVAL, "checkpoint spacing must be >= 0");
+    e->grad_ckpt = every;
+    return CF_OK;
+}
+
+size_t cf_grad_arena_bytes(int32_t L, int32_t every) {
+    if (L < 0 || L > CF_MAX_LEN) return 0;
+    if (every <= 0) every = cf::adj_auto_checkpoint(L);
+    return sizeof(float) * (size_t)arena_words(JOB_GRAD, L, every);
+}
+
 int cf_logz(cf_engine* e, const uint8_t* seqs, const int64_t* offsets, const uint8_t* mask, int32_t n,
             float* logz_out) {
     if (n > 0 && !logz_out) return fail(CF_EINVAL, "logz_out is NULL");
@@ -1091,7 +1107,14 @@ extern "C" int cf_grad(cf_engine* e, const uint8_t* seqs, const int64_t* offsets
     for (int64_t w : P.slice_words) maxw = std::max(maxw, w);
     if ((rc = e->arena.ensure((size_t)maxw))) return rc;
     const size_t smem = cf::adj_smem_bytes(P.Lmax);
-    if (smem > 48 * 1024 - CF_BLOB_LEN * 8) return fail(CF_EINVAL, "sequence too long for the adjoint kernels");
+    {
+        int dev_max = 0;
+        CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
+        if (smem > (size_t)dev_max) return fail(CF_EINVAL, "sequence too long for the adjoint kernels");
+        for (const void* k : {(const void*)cf::k_adj_inside, (const void*)cf::k_adj_outside})
+            CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::max<size_t>(smem, 48 * 1024)));
+    }
     for (size_t sl = 0; sl + 1 < P.slice_begin.size(); ++sl) {
         const int k0 = P.slice_begin[sl], k1 = P.slice_begin[sl + 1];
         cf::FoldArgs A;
@@ -1110,9 +1133,8 @@ extern "C" int cf_grad(cf_engine* e, const uint8_t* seqs, const int64_t* offsets
         A.post_offs = nullptr;
         A.gamma = 0.f;
         A.status = e->status.p;
-        cf::k_adj_inside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus);
-        cf::k_adj_outside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus);
-        cf::k_adj_counts<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus, e->counts.p, e->unpaired.p);
+        cf::k_adj_inside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus, P.grad_ckpt);
+        cf::k_adj_outside<<<A.n, cf::kFoldThreads, smem, st>>>(A, d_bonus, P.grad_ckpt, e->counts.p, e->unpaired.p);
         CF_CUDA(cudaGetLastError());
     }
     CF_CUDA(cudaMemcpyAsync(counts_out, e->counts.p, sizeof(double) * n * CF_BLOB_LEN, cudaMemcpyDeviceToHost, st));

@@ -145,6 +145,12 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 #endif
 constexpr int kChainPF = CF_CHAIN_PF;
 constexpr int kChainAsync = CF_CHAIN_ASYNC;
+// CF_FLAT_WALK = 1 walks the single-branch windows (inside_B, outside_B,
+// posterior_pair) in flattened lockstep (each lane on its own row sequence),
+// 0 in row lockstep.  Results are identical.
+#ifndef CF_FLAT_WALK
+#define CF_FLAT_WALK 0
+#endif
 // CF_CHAIN_UNROLL = 1 unrolls the asynchronous pipeline over its ring slots
 // (constant slot addresses, more code)
 #ifndef CF_CHAIN_UNROLL
@@ -405,9 +411,68 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
     const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
     const R jB = tb->jB[idx4(si, sj1, si1, sj)];
     R acc = sr.plus(NEG, S::add(jB, P.hp(d <= DHP ? d : DHP)));
+    const int nrows = (d < CMAX ? d : CMAX) + 1;
+    // one single-branch candidate: inner pair (p+1, q) of row l1, table value v
+    auto fold = [&](int l1, int q, R sn0, R sn1, R v) {
+        // no zero-threshold test on v: a visited candidate is a pairable
+        // cell, whose FC always holds its hairpin term, and acc (likewise) is
+        // finite, so a sub-threshold v would leave acc unchanged in any case
+        const int p = i + l1;
+        const int l2 = j - q, a = p + 1;
+        R e;
+        if (l1 == 0 && l2 == 0) {
+            e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
+        } else {
+            const int sq = Q.s[q], sa = Q.s[a];
+            const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
+            const R snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : R(0));
+            e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
+        }
+        acc = sr.plus(acc, S::add(e, v));
+    };
+#if CF_FLAT_WALK
+    // Flattened lockstep: each lane walks its own candidate sequence (rows
+    // l1 ascending, q descending within a row) and moves to its next row as
+    // soon as its row is exhausted, so a lane idles only once it has no
+    // candidates left -- not at the end of every row, as the row-lockstep
+    // walk does.  The next candidate's table value is loaded before the
+    // current one is folded.
+    int l1 = -1, qlo = 0;
+    uint32_t msk = 0u;
+    R sn0 = R(0), sn1 = R(0);
+    auto next = [&](int& ql1, int& qq, R& q0, R& q1) -> bool {
+        while (msk == 0u) {
+            if (++l1 >= nrows) return false;
+            const int p = i + l1;
+            qlo = (p + 2 > l1 + j - CMAX) ? p + 2 : l1 + j - CMAX;
+            msk = Q.window(p + 1, qlo, j - qlo + 1);
+            sn0 = l1 == 1 ? P.b01(si1) : R(0);
+            sn1 = l1 == 0 ? P.b01(sj) : (l1 == 1 ? P.i11(si1, sj) : R(0));
+        }
+        const int bit = 31 - __clz(msk);
+        msk ^= 1u << bit;
+        ql1 = l1;
+        qq = qlo + bit;
+        q0 = sn0;
+        q1 = sn1;
+        return true;
+    };
+    int cl1 = 0, cq = 0;
+    R c0 = R(0), c1 = R(0), cv = R(0);
+    bool have = next(cl1, cq, c0, c1);
+    if (have) cv = T.FC[tri_off(cq - 2 - (i + cl1), m) + i + cl1 + 1];
+    while (__any_sync(lanes, have)) {
+        int nl1 = 0, nq = 0;
+        R n0 = R(0), n1 = R(0), nv = R(0);
+        const bool hn = have && next(nl1, nq, n0, n1);
+        if (hn) nv = T.FC[tri_off(nq - 2 - (i + nl1), m) + i + nl1 + 1];
+        if (have) fold(cl1, cq, c0, c1, cv);
+        have = hn;
+        cl1 = nl1; cq = nq; c0 = n0; c1 = n1; cv = nv;
+    }
+#else
     // rows p = i + l1, l1 = 0 .. min(30, d); row q range [qlo, j],
     // qlo = max(p + 2, l1 + j - 30)
-    const int nrows = (d < CMAX ? d : CMAX) + 1;
     const int nr = __reduce_max_sync(lanes, nrows);
     for (int l1 = 0; l1 < nr; ++l1) {
         const int p = i + l1;
@@ -419,25 +484,9 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
         const int slots = __reduce_max_sync(lanes, __popc(msk));
         lockstep_row<true, R>(
             msk, slots, [&](int bit) -> R { return T.FC[tri_off(qlo + bit - 2 - p, m) + p + 1]; },
-            [&](int bit, R v) {
-                // no zero-threshold test on v: a visited candidate is a
-                // pairable cell, whose FC always holds its hairpin term, and
-                // acc (likewise) is finite, so a sub-threshold v would leave
-                // acc unchanged in any case
-                const int q = qlo + bit;
-                const int l2 = j - q, a = p + 1;
-                R e;
-                if (l1 == 0 && l2 == 0) {
-                    e = S::add(P.bp(si1, sj), P.stack(si, sj1, si1, sj));
-                } else {
-                    const int sq = Q.s[q], sa = Q.s[a];
-                    const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
-                    const R snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : R(0));
-                    e = S::add(S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2), snuc);
-                }
-                acc = sr.plus(acc, S::add(e, v));
-            });
+            [&](int bit, R v) { fold(l1, qlo + bit, sn0, sn1, v); });
     }
+#endif
     if (fm2 > HALF) {
         const R jA = junctionA<S>(P, L, Q, i, j);
         acc = sr.plus(acc, S::add(S::add(S::add(fm2, jA), P.mp()), P.mb()));

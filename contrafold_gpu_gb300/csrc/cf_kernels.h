@@ -70,13 +70,13 @@ __global__ void k_plain_posterior32(FoldArgs A);
 __global__ void k_plain_mea32(FoldArgs A);
 size_t plain_smem_bytes(int Lmax);
 
-// Adjoint (cf_adjoint.cu): inside/outside with a soft unpaired bonus and the
-// expected-count pass.
-__global__ void k_adj_inside(FoldArgs A, const float* bonus);
-__global__ void k_adj_outside(FoldArgs A, const float* bonus);
-__global__ void k_adj_counts(FoldArgs A, const float* bonus, double* counts_out, double* unpaired_out);
+// Adjoint (cf_adjoint.cu): inside with a soft unpaired bonus (FM2 kept on
+// every ckpt-th diagonal), then the outside with the expected counts folded in.
+__global__ void k_adj_inside(FoldArgs A, const float* bonus, int ckpt);
+__global__ void k_adj_outside(FoldArgs A, const float* bonus, int ckpt, double* counts_out, double* unpaired_out);
 size_t adj_smem_bytes(int Lmax);
-int64_t adj_arena_words(int L);
+int64_t adj_arena_words(int L, int ckpt);
+int adj_auto_checkpoint(int L);
 
 // Persistent fused per-sequence kernel (one CTA per sequence at a time).
 enum { kCtaLogZ = 0, kCtaMea = 1, kCtaBpp = 2 };

@@ -268,8 +268,48 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
         }
         acc = sr.plus(acc, __fadd_rn(v, e));
     };
-    const int lm = __reduce_max_sync(lanes, l1max + 1) - 1;
     uint32_t m0 = 0u;
+#if CF_FLAT_WALK
+    // flattened lockstep (see inside_B): rows l1max .. 0 of this lane, within a
+    // row highest j first; row 0 without its stacking source
+    {
+        int l1 = l1max + 1;
+        uint32_t msk = 0u;
+        float sn0 = 0.0f, sn1 = 0.0f;
+        auto next = [&](int& ql1, int& qj, float& q0, float& q1) -> bool {
+            while (msk == 0u) {
+                if (--l1 < 0) return false;
+                msk = rowmask(l1);
+                if (l1 == 0) {
+                    m0 = msk;
+                    msk &= ~1u;   // the stacking source comes after the FM1o term
+                }
+                snuc_row(l1, sn0, sn1);
+            }
+            const int bit = 31 - __clz(msk);
+            msk ^= 1u << bit;
+            ql1 = l1;
+            qj = b + 1 + bit;
+            q0 = sn0;
+            q1 = sn1;
+            return true;
+        };
+        int cl1 = 0, cj = 0;
+        float c0 = 0.0f, c1 = 0.0f, cv = 0.0f;
+        bool have = next(cl1, cj, c0, c1);
+        if (have) cv = src_val(cl1, cj);
+        while (__any_sync(lanes, have)) {
+            int nl1 = 0, nj = 0;
+            float n0 = 0.0f, n1 = 0.0f, nv = 0.0f;
+            const bool hn = have && next(nl1, nj, n0, n1);
+            if (hn) nv = src_val(nl1, nj);
+            if (have) source(cl1, cj, cv, c0, c1);
+            have = hn;
+            cl1 = nl1; cj = nj; c0 = n0; c1 = n1; cv = nv;
+        }
+    }
+#else
+    const int lm = __reduce_max_sync(lanes, l1max + 1) - 1;
     for (int l1 = lm; l1 >= 0; --l1) {
         uint32_t msk = l1 <= l1max ? rowmask(l1) : 0u;
         if (l1 == 0) {
@@ -283,6 +323,7 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             msk, slots, [&](int bit) { return src_val(l1, b + 1 + bit); },
             [&](int bit, float v) { source(l1, b + 1 + bit, v, sn0, sn1); });
     }
+#endif
     if (l1max >= 0) {
         if (b + 1 < L) {
             const float v = T.FM1o[tri_off(t + 2, m) + a - 1];
@@ -362,6 +403,43 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
         }
         m0 &= ~1u;
     }
+#if CF_FLAT_WALK
+    // flattened lockstep (see inside_B): rows 0 .. l1max of this lane, within
+    // a row lowest j first
+    {
+        int l1 = 0;
+        uint32_t msk = m0;
+        float sn0 = 0.0f, sn1 = 0.0f;
+        snuc_row(0, sn0, sn1);
+        auto next = [&](int& ql1, int& qj, float& q0, float& q1) -> bool {
+            while (msk == 0u) {
+                if (++l1 > l1max) return false;
+                msk = rowmask(l1);
+                snuc_row(l1, sn0, sn1);
+            }
+            const int bit = __ffs(msk) - 1;
+            msk &= msk - 1u;
+            ql1 = l1;
+            qj = b + bit;
+            q0 = sn0;
+            q1 = sn1;
+            return true;
+        };
+        int cl1 = 0, cj = 0;
+        float c0 = 0.0f, c1 = 0.0f, cv = 0.0f;
+        bool have = next(cl1, cj, c0, c1);
+        if (have) cv = src_val(cl1, cj);
+        while (__any_sync(lanes, have)) {
+            int nl1 = 0, nj = 0;
+            float n0 = 0.0f, n1 = 0.0f, nv = 0.0f;
+            const bool hn = have && next(nl1, nj, n0, n1);
+            if (hn) nv = src_val(nl1, nj);
+            if (have) source(cl1, cj, cv, c0, c1);
+            have = hn;
+            cl1 = nl1; cj = nj; c0 = n0; c1 = n1; cv = nv;
+        }
+    }
+#else
     const int lm = __reduce_max_sync(lanes, l1max + 1) - 1;
     for (int l1 = 0; l1 <= lm; ++l1) {
         uint32_t msk = l1 == 0 ? m0 : (l1 <= l1max ? rowmask(l1) : 0u);
@@ -372,6 +450,7 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
             msk, slots, [&](int bit) { return src_val(l1, b + bit); },
             [&](int bit, float v) { source(l1, b + bit, v, sn0, sn1); });
     }
+#endif
     if (!live) return 0.0f;
     const float outside = __fsub_rn(T.F5o[b], Z);
     const float f5k = T.F5[a - 1];

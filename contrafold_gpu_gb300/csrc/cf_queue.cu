@@ -21,7 +21,8 @@
 // claim word is published (fence, then an atomic exchange), and a claimer
 // fences after its claim before it reads them.  Waits for work are polls of
 // shared memory bounded in time: a warp that finds no work for kIdleLimitNs
-// sets CF_ETIMEOUT and leaves (the rest of the CTA then runs out of work too).
+// sets CF_ETIMEOUT and leaves (the rest of the CTA then runs out of work too),
+// and no warp schedules work for longer than kLaunchLimitNs.
 //
 // Per-cell arithmetic is the one of the other schedules (cf_inside.cuh,
 // cf_outside.cuh, cf_mea.cuh, cf_sample.cuh): results are identical, bit for
@@ -65,6 +66,9 @@ struct QueueSmemHead {
 
 constexpr int kQueueWarps = kQueueThreads / 32;
 constexpr unsigned long long kIdleLimitNs = 20ull * 1000 * 1000 * 1000;   // 20 s without any work: give up
+// a launch that is still scheduling after this long has lost its way: every
+// warp gives up at its next poll, with CF_ETIMEOUT
+constexpr unsigned long long kLaunchLimitNs = 120ull * 1000 * 1000 * 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;
@@ -492,7 +496,12 @@ __global__ void __launch_bounds__(kQueueThreads, kQueueMinBlocks) k_fold_queue(Q
 
     int rot = warp;
     unsigned long long idle_since = 0;
+    const unsigned long long t_start = globaltimer();
     for (;;) {
+        if (globaltimer() - t_start > kLaunchLimitNs) {
+            if (lane == 0) atomicExch(A.status, CF_ETIMEOUT);
+            break;
+        }
         // find a claimable chunk, starting at a per-warp rotating seat
         int got_seat = -1, got_chunk = 0;
         unsigned got_gen = 0;

@@ -27,7 +27,8 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
            "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_group", "cf_engine_load_tuning",
-           "cf_engine_tuning_rows", "cf_last_error", "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
+           "cf_engine_tuning_rows", "cf_engine_set_grad_checkpoint", "cf_grad_arena_bytes", "cf_last_error",
+           "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_sample_tasks", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group", "cf_plan_set_graph", "cf_plan_schedule", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
@@ -66,6 +67,10 @@ def load_library(path: str = LIB_PATH):
         L.cf_engine_set_group.argtypes = [vp, ctypes.c_int]
         L.cf_engine_load_tuning.argtypes = [vp, ctypes.c_char_p]
         L.cf_engine_tuning_rows.argtypes = [vp]
+        L.cf_engine_set_grad_checkpoint.argtypes = [vp, ctypes.c_int32]
+        L.cf_engine_set_grad_checkpoint.restype = ctypes.c_int
+        L.cf_grad_arena_bytes.argtypes = [ctypes.c_int32, ctypes.c_int32]
+        L.cf_grad_arena_bytes.restype = ctypes.c_size_t
         L.cf_last_error.restype = ctypes.c_char_p
         L.cf_version.restype = ctypes.c_char_p
         L.cf_logz.argtypes = [vp, u8p, i64p, u8p, ctypes.c_int32, f32p]
@@ -205,6 +210,12 @@ class Engine:
     def tuning_rows(self) -> int:
         return int(self.lib.cf_engine_tuning_rows(self._h))
 
+    def set_grad_checkpoint(self, every: int = 0):
+        """cf_grad keeps the inside FM2 on every `every`-th diagonal and
+        recomputes the rest (1: all kept; 0: automatic).  Results are bitwise
+        the same for every spacing."""
+        self._check(self.lib.cf_engine_set_grad_checkpoint(self._h, int(every)))
+
     # ---- batch entry points ----
     def _args(self, B: Batch):
         return (self._h, _p(B.buf, ctypes.c_uint8) if B.total else None, _p(B.offsets, ctypes.c_int64),
@@ -279,6 +290,11 @@ class Engine:
             self._check(self.lib.cf_sample_tasks(*self._args(B), ctypes.c_int32(int(chunk)),
                                                  ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
         return B.split_strings(out.raw[:B.total])
+
+
+def grad_arena_bytes(L: int, every: int = 0) -> int:
+    """Device bytes cf_grad uses for one sequence of L nt."""
+    return int(load_library().cf_grad_arena_bytes(int(L), int(every)))
 
 
 class Plan:

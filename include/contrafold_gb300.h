@@ -195,13 +195,24 @@ int cf_sample_tasks(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
  * unpaired position, returns per sequence b:
  *   logz_out[b]                          logZ (accurate float32 log-sum-exp)
  *   counts_out[b*CF_BLOB_LEN + e]        d logZ / d(parameter-blob entry e) =
- *                                        expected uses of entry e (FP64 sums)
+ *                                        expected uses of entry e (exact sums)
  *   unpaired_out[offsets[b] + t]         d logZ / d bonus_t = P(t unpaired)
  * The raw-feature gradient is counts_out times the tying Jacobian of the
  * loader (linear, gpu_contrafold/cpu.py:40-135). */
 int cf_grad(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
             const uint8_t* mask, int32_t n, const float* bonus, float* logz_out,
             double* counts_out, double* unpaired_out);
+/* Memory of cf_grad (no reference counterpart).  The inside tables FC, FM,
+ * FM1 and the outside FM2o stay whole; FCo, FMo, FM1o live in ring buffers of
+ * a few diagonals (the expected counts are taken one diagonal behind the
+ * outside pass); the inside FM2 is kept on every `every`-th diagonal and
+ * recomputed on the others (every = 1: all kept; 0: automatic -- 1 below
+ * 512 nt, else 8).  The counts are summed in exact 128-bit fixed point, so
+ * the results are bitwise the same for every spacing and every run. */
+int cf_engine_set_grad_checkpoint(cf_engine* eng, int32_t every);
+/* Device bytes cf_grad uses per sequence of L nt at checkpoint spacing
+ * `every` (0: automatic); 0 for a bad length. */
+size_t cf_grad_arena_bytes(int32_t L, int32_t every);
 
 /* ---- plans: device-resident batches ----
  * A plan fixes a batch's shape (lengths from host `offsets`), orders and
