@@ -542,9 +542,11 @@ def serving_arm(args):
            "config": {"workload": "serving: Poisson arrivals, lengths log-normal median 150 nt sigma 0.6 clipped 30-1000, "
                                   "40% logZ / 40% MEA / 20% sample x10, 10% masked",
                       "workers": args.workers, "long_workers": args.long_workers, "long_len": args.long_len,
-                      "edges": args.edges}}
+                      "edges": args.edges, "max_batch_cost": args.max_batch_cost,
+                      "max_batch_arena": args.max_batch_arena}}
     with serve.Server(P, workers=args.workers, long_workers=args.long_workers, long_len=args.long_len,
-                      edges=args.edges) as srv:
+                      edges=args.edges, max_batch_cost=args.max_batch_cost,
+                      max_batch_arena=args.max_batch_arena) as srv:
         warm, _ = serve.mixed_workload(2000, rate=1e9, seed=99)
         srv.replay(warm, np.zeros(len(warm)), keep_results=False)
         n_sat = args.serve_n
@@ -766,6 +768,10 @@ def main():
     ap.add_argument("--long-len", type=int, default=256, help="serving: buckets above this length are long")
     ap.add_argument("--edges", type=int, nargs="+", default=[96, 192, 256, 384, 640],
                     help="serving: length-bucket upper edges")
+    ap.add_argument("--max-batch-cost", type=float, default=0.0,
+                    help="serving: cap on a batch's predicted work, sum of L^3 (0 = none)")
+    ap.add_argument("--max-batch-arena", type=int, default=0,
+                    help="serving: cap on a batch's device arena bytes (0 = none)")
     ap.add_argument("--serve-n", type=int, default=20000, help="serving: requests of the saturation run")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: seconds of arrivals per load point")
     ap.add_argument("--serve-fracs", type=float, nargs="+", default=[0.2, 0.5, 0.8, 0.9])

@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "../../include/contrafold_gb300.h"
+#include "cf_device.cuh"
 #include "cf_host.h"
 
 namespace {
@@ -89,6 +90,8 @@ struct cf_server {
     bool paused = false;
     int32_t max_batch = 4096;
     int64_t max_batch_nt = int64_t(1) << 20;
+    double max_batch_cost = 0;          // predicted work of a batch, sum of L^3 (0 = no limit)
+    int64_t max_batch_arena = 0;        // device arena bytes of a batch (0 = no limit)
     int32_t long_len = 256;              // buckets whose upper edge is above this are long
     int32_t long_workers = 1;            // workers [0, long_workers) may take long batches
     std::vector<int32_t> edges{96, 192, 256, 384, 640};
@@ -108,6 +111,13 @@ struct cf_server {
 };
 
 namespace {
+
+// Device arena bytes one request of L nt takes in a batched call: the full
+// FP32 fold arena for MEA, its inside-only prefix for logZ and sampling.
+int64_t request_arena_bytes(int op, int L) {
+    const int64_t w = op == CF_OP_MEA ? cf::arena32(L).total : cf::arena32_inside_words(L);
+    return 4 * w;
+}
 
 // Folds one batch on `eng`; fills each request's outputs and status.
 void run_batch(cf_server* S, cf_engine* eng, const Key& key, std::vector<Req*>& batch, std::vector<uint8_t>& buf,
@@ -189,15 +199,27 @@ void worker_loop(cf_server* S, int w) {
             key = best->first;
             auto& q = best->second;
             batch.clear();
-            int64_t nt = 0;
-            while (!q.empty() && (int)batch.size() < S->max_batch &&
-                   (batch.empty() || nt + (int64_t)q.front()->seq.size() <= S->max_batch_nt)) {
+            int64_t nt = 0, arena = 0;
+            double cost = 0;
+            // oldest first, while the batch stays within its count, nucleotide,
+            // predicted-work (sum of L^3: the fold is cubic in the length) and
+            // arena-byte limits; the first request is always taken
+            while (!q.empty() && (int)batch.size() < S->max_batch) {
                 Req* r = q.front();
+                const int64_t L = (int64_t)r->seq.size();
+                const double c = (double)L * (double)L * (double)L;
+                const int64_t a = request_arena_bytes(key.op, (int)L);
+                if (!batch.empty() && (nt + L > S->max_batch_nt ||
+                                       (S->max_batch_cost > 0 && cost + c > S->max_batch_cost) ||
+                                       (S->max_batch_arena > 0 && arena + a > S->max_batch_arena)))
+                    break;
                 q.pop_front();
                 --S->queued;
                 if (long_batch) --S->queued_long;
                 r->state = kRunning;
-                nt += (int64_t)r->seq.size();
+                nt += L;
+                cost += c;
+                arena += a;
                 batch.push_back(r);
             }
             if (q.empty()) S->queues.erase(best);
@@ -338,6 +360,15 @@ int cf_server_configure(cf_server* S, int32_t max_batch, int64_t max_batch_nt, i
     S->long_len = long_len;
     S->long_workers = long_workers;
     S->edges.assign(edges, edges + n_edges);
+    return CF_OK;
+}
+
+int cf_server_set_limits(cf_server* S, double max_batch_cost, int64_t max_batch_arena_bytes) {
+    if (!S) return fail(CF_EINVAL, "server is NULL");
+    if (!(max_batch_cost >= 0) || max_batch_arena_bytes < 0) return fail(CF_EINVAL, "limits must be >= 0");
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->max_batch_cost = max_batch_cost;
+    S->max_batch_arena = max_batch_arena_bytes;
     return CF_OK;
 }
 

@@ -32,7 +32,8 @@ SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_sample_tasks", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
            "cf_plan_run", "cf_plan_status", "cf_plan_set_timing", "cf_plan_phase_ms", "cf_plan_launches",
            "cf_plan_group", "cf_plan_set_graph", "cf_plan_schedule", "cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
-           "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats")
+           "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats",
+           "cf_server_set_limits")
 CF_JOB_LOGZ, CF_JOB_LOGZ64, CF_JOB_BPP, CF_JOB_MEA, CF_JOB_MFE = 0, 1, 2, 3, 4
 
 

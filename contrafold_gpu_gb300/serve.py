@@ -73,6 +73,7 @@ def _bind(L):
     L.cf_server_configure.argtypes = [vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                       P(ctypes.c_int32), ctypes.c_int32]
     L.cf_server_pause.argtypes = [vp, ctypes.c_int32]
+    L.cf_server_set_limits.argtypes = [vp, ctypes.c_double, ctypes.c_int64]
     L.cf_server_submit.argtypes = [vp, P(_CRequest), u8p, ctypes.c_int32, u8p, P(ctypes.c_int64)]
     L.cf_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, P(ctypes.c_float), ctypes.c_char_p,
                                  ctypes.c_int64]
@@ -80,7 +81,7 @@ def _bind(L):
     L.cf_server_replay.argtypes = [vp, ctypes.c_int32, P(ctypes.c_double), P(_CRequest), u8p, i64p, u8p, i64p,
                                    P(ctypes.c_float), ctypes.c_char_p, P(ctypes.c_double), P(ctypes.c_int32)]
     L.cf_server_stats.argtypes = [vp, P(ctypes.c_double), ctypes.c_int32]
-    for name in ("cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause",
+    for name in ("cf_server_create", "cf_server_destroy", "cf_server_configure", "cf_server_pause", "cf_server_set_limits",
                  "cf_server_submit", "cf_server_wait", "cf_server_cancel", "cf_server_replay", "cf_server_stats"):
         getattr(L, name).restype = ctypes.c_int
     L._cf_server_typed = True
@@ -99,7 +100,8 @@ class Server:
 
     def __init__(self, P: dict, device: int = 0, workers: int = 6, max_batch: int = 4096,
                  max_batch_nt: int = 1 << 20, long_len: int = 256, long_workers: int = 2,
-                 edges: Sequence[int] = (96, 192, 256, 384, 640)):
+                 edges: Sequence[int] = (96, 192, 256, 384, 640), max_batch_cost: float = 0.0,
+                 max_batch_arena: int = 0):
         self.lib = _bind(load_library())
         b32, b64 = _params.pack32(P), _params.pack64(P)
         self._h = ctypes.c_void_p()
@@ -109,6 +111,11 @@ class Server:
         e = np.asarray(edges, np.int32)
         self._check(self.lib.cf_server_configure(self._h, int(max_batch), int(max_batch_nt), int(long_len),
                                                  int(min(long_workers, workers)), _p(e, ctypes.c_int32), int(e.size)))
+        self.set_limits(max_batch_cost, max_batch_arena)
+
+    def set_limits(self, max_batch_cost: float = 0.0, max_batch_arena: int = 0):
+        """Cap a batch's predicted work (sum of L^3) and its device arena bytes (0 = no cap)."""
+        self._check(self.lib.cf_server_set_limits(self._h, float(max_batch_cost), int(max_batch_arena)))
 
     def _check(self, rc):
         if rc != CF_OK:

@@ -292,6 +292,13 @@ int cf_server_destroy(cf_server* server);
 int cf_server_configure(cf_server* server, int32_t max_batch, int64_t max_batch_nt,
                         int32_t long_len, int32_t long_workers, const int32_t* edges,
                         int32_t n_edges);
+/* Batch limits by cost: a worker stops adding requests (oldest first) to a
+ * batch when the sum of L^3 over its requests -- the predicted work, the fold
+ * being cubic in the length -- would pass max_batch_cost, or the device arena
+ * the batch needs (the FP32 fold arena per MEA request, its inside part per
+ * logZ / sampling request) would pass max_batch_arena_bytes; 0 = no limit.
+ * The first request of a batch is always taken.  Any time. */
+int cf_server_set_limits(cf_server* server, double max_batch_cost, int64_t max_batch_arena_bytes);
 /* While paused, workers start no new batch (requests keep queueing). */
 int cf_server_pause(cf_server* server, int32_t on);
 /* Copies the sequence (and mask: NULL or len bytes, != 0 forces unpaired). */
