@@ -11,6 +11,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <sstream>
 #include <string>
@@ -75,6 +77,22 @@ struct DevBuf {
         cap = 0;
     }
 };
+
+// The dynamic shared-memory limit is an attribute of a kernel function, shared
+// by every engine of the process, so it is raised here, process-wide and per
+// device, and never lowered: an engine asking for less must not take away what
+// another engine's launches rely on.
+std::mutex g_smem_mu;
+std::map<std::pair<const void*, int>, size_t> g_smem_set;
+
+int raise_smem_limit(const void* fn, int device, size_t bytes) {
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    size_t& cur = g_smem_set[{fn, device}];
+    if (bytes <= cur) return CF_OK;
+    CF_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+    return CF_OK;
+}
 
 enum Job { JOB_LOGZ = 0, JOB_LOGZ64, JOB_BPP, JOB_MEA, JOB_MFE, JOB_SAMPLE, JOB_GRAD };
 
@@ -287,7 +305,9 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         const int Lmed = n ? (int)(offsets[order[n / 2] + 1] - offsets[order[n / 2]]) : 0;
         int sms = 0;
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
-        const int slots = std::max(1, cf::kFoldMinBlocks * sms);
+        // resident CTAs per SM of the kernel that will run: the fused MEA kernel
+        // is built for more than the other grouped kernels
+        const int slots = std::max(1, (job == JOB_MEA ? cf::kFoldMinBlocksMea : cf::kFoldMinBlocks) * sms);
         // whole waves: the fewest waves whose groups fit kMaxGroup sequences
         const int waves = std::max(1, (n + cf::kMaxGroup * slots - 1) / (cf::kMaxGroup * slots));
         const int wave_group = std::min(cf::kMaxGroup, std::max(1, (n + waves * slots - 1) / (waves * slots)));
@@ -464,24 +484,23 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     int dev_max = 0;
     CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device));
     if ((size_t)dev_max < bytes) return fail(CF_EINVAL, "sequence too long for shared-memory staging");
-    const void* ks[] = {(const void*)cf::k_plain_inside32, (const void*)cf::k_plain_outside32,
-                        (const void*)cf::k_plain_posterior32, (const void*)cf::k_plain_mea32,
-                        (const void*)cf::k_inside64, (const void*)cf::k_viterbi64};
-    for (const void* k : ks) CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    std::vector<const void*> ks = {(const void*)cf::k_plain_inside32, (const void*)cf::k_plain_outside32,
+                                   (const void*)cf::k_plain_posterior32, (const void*)cf::k_plain_mea32,
+                                   (const void*)cf::k_inside64, (const void*)cf::k_viterbi64};
     for (bool wide : {false, true}) {
         const cf::FoldKernels fk = cf::fold_kernels(wide);
         for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea, fk.fused_mea, fk.fused_bpp})
-            CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+            ks.push_back((const void*)k);
     }
-    for (int mode = 0; mode < 4; ++mode)
-        CF_CUDA(cudaFuncSetAttribute(cf::warp_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    for (int mode = 0; mode < 3; ++mode)
-        CF_CUDA(cudaFuncSetAttribute(cf::cta_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    for (int mode = 0; mode < 4; ++mode)
-        CF_CUDA(cudaFuncSetAttribute(cf::queue_kernel(mode), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (int mode = 0; mode < 4; ++mode) ks.push_back(cf::warp_kernel(mode));
+    for (int mode = 0; mode < 3; ++mode) ks.push_back(cf::cta_kernel(mode));
+    for (int mode = 0; mode < 4; ++mode) ks.push_back(cf::queue_kernel(mode));
     const cf::ClusterKernels ck = cf::cluster_kernels();
-    for (cf::FoldKernel k : {ck.mea, ck.bpp, ck.inside_acc})
-        CF_CUDA(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    for (cf::FoldKernel k : {ck.mea, ck.bpp, ck.inside_acc}) ks.push_back((const void*)k);
+    for (const void* k : ks) {
+        const int rc = raise_smem_limit(k, eng->device, bytes);
+        if (rc) return rc;
+    }
     eng->smem_optin = bytes;
     return CF_OK;
 }
@@ -764,9 +783,7 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                 S.out = sj->d_out;
                 S.status = X.status;
                 const size_t ssm = cf::sample_smem_bytes(P.Lmax);
-                if (ssm > 48 * 1024)
-                    CF_CUDA(cudaFuncSetAttribute((const void*)cf::k_sample32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)ssm));
+                if (ssm > 48 * 1024 && (rc = raise_smem_limit((const void*)cf::k_sample32, eng->device, ssm))) return rc;
                 const int64_t items = (int64_t)A.n * sj->n_samples;
                 const int warps = cf::sample_threads() / 32;
                 const int sgrid = (int)std::min<int64_t>((items + warps - 1) / warps, 152 * 16);
@@ -1111,9 +1128,10 @@ extern "C" int cf_grad(cf_engine* e, const uint8_t* seqs, const int64_t* offsets
         int dev_max = 0;
         CF_CUDA(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
         if (smem > (size_t)dev_max) return fail(CF_EINVAL, "sequence too long for the adjoint kernels");
-        for (const void* k : {(const void*)cf::k_adj_inside, (const void*)cf::k_adj_outside})
-            CF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)std::max<size_t>(smem, 48 * 1024)));
+        for (const void* k : {(const void*)cf::k_adj_inside, (const void*)cf::k_adj_outside}) {
+            const int rs = raise_smem_limit(k, e->device, std::max<size_t>(smem, 48 * 1024));
+            if (rs) return rs;
+        }
     }
     for (size_t sl = 0; sl + 1 < P.slice_begin.size(); ++sl) {
         const int k0 = P.slice_begin[sl], k1 = P.slice_begin[sl + 1];

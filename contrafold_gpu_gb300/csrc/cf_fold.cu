@@ -501,7 +501,8 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k
 // is done, instead of every phase waiting for the slowest CTA of the grid.
 // ---------------------------------------------------------------------------
 template <int NT, int MODE>
-__global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k_fold_group32(FoldArgs A) {
+__global__ void __launch_bounds__(NT, NT == kFoldThreads ? (MODE == 0 ? kFoldMinBlocksMea : kFoldMinBlocks) : 1)
+    k_fold_group32(FoldArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto* sm = reinterpret_cast<SmemFold<float>*>(smem_raw);
     setup_group(sm, A, A.blob32);

@@ -137,10 +137,8 @@ __device__ __forceinline__ typename S::Real junctionA_rev(const ParamView<typena
 //     default of the PFD template parameter; latency kernels pass a deeper one).
 //   both 0: load, then fold.
 // ---------------------------------------------------------------------------
-// (GB300, grouped fold at 4 CTAs per SM: depth 2 -> 33.1k, 3 -> 33.9k, 4 -> 33.2k,
-// 6 -> 31.5k 200-nt MEA folds/s)
 #ifndef CF_CHAIN_PF
-#define CF_CHAIN_PF 3
+#define CF_CHAIN_PF 4
 #endif
 #ifndef CF_CHAIN_ASYNC
 #define CF_CHAIN_ASYNC 0

@@ -9,12 +9,17 @@
 namespace cf {
 
 constexpr int kFoldThreads = 256;       // threads per fold CTA
-// resident CTAs per SM the register budget targets (GB300, 10,000 x 200 nt MEA:
-// 2 -> 23.5k, 3 -> 31.9k, 4 -> 33.9k, 5 -> 29.3k folds/s; 4 U{40..400} nt: 16.5k)
 #ifndef CF_FOLD_MIN_BLOCKS
-#define CF_FOLD_MIN_BLOCKS 4
+#define CF_FOLD_MIN_BLOCKS 3
 #endif
-constexpr int kFoldMinBlocks = CF_FOLD_MIN_BLOCKS;
+constexpr int kFoldMinBlocks = CF_FOLD_MIN_BLOCKS;   // resident CTAs per SM the register budget targets
+// ... and for the fused grouped MEA kernel alone (GB300, 10,000 x 200 nt MEA:
+// 3 -> 31.9k, 4 -> 33.2k folds/s, 40-400 nt 14.4k -> 16.3k; 4 slowed the
+// per-phase kernels, the fused BPP kernel and the sampler's inside 1.5-2.5x)
+#ifndef CF_FOLD_MIN_BLOCKS_MEA
+#define CF_FOLD_MIN_BLOCKS_MEA 4
+#endif
+constexpr int kFoldMinBlocksMea = CF_FOLD_MIN_BLOCKS_MEA;
 constexpr int kFoldThreadsWide = 512;   // per-phase fold CTA when the grid has at most one CTA per SM:
                                         // a long sequence's diagonal spreads over twice the threads
 constexpr int kMaxGroup = 32;       // sequences per CTA on the batched path

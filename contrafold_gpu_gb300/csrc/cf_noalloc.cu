@@ -221,8 +221,22 @@ extern "C" int cf_mea_scratch(cf_engine* e, const uint8_t* seqs, const int64_t* 
     W.out = nullptr;
     W.status = status;
     void* args[] = {&W};
-    CF_CUDA_Q(cudaLaunchKernel(cf::warp_kernel(mode), dim3((unsigned)grid), dim3(cf::kWarpThreads), args, smem, st));
-    CF_CUDA_Q(cudaGetLastError());
+    {
+        const cudaError_t le = cudaLaunchKernel(cf::warp_kernel(mode), dim3((unsigned)grid), dim3(cf::kWarpThreads),
+                                                args, smem, st);
+        if (le != cudaSuccess) {   // report the launch shape with the error
+            cudaFuncAttributes fa{};
+            cudaFuncGetAttributes(&fa, cf::warp_kernel(mode));
+            char m[320];
+            std::snprintf(m, sizeof m,
+                          "cf_mea_scratch: launch of %lld CTAs with %zu bytes of dynamic shared memory failed: %s "
+                          "(kernel: %zu bytes static, %d allowed dynamic, %d registers)",
+                          (long long)grid, smem, cudaGetErrorString(le), fa.sharedSizeBytes,
+                          fa.maxDynamicSharedSizeBytes, fa.numRegs);
+            (void)cudaStreamSynchronize(st);
+            return cf::engine_fail(CF_ECUDA, m);
+        }
+    }
 
     int h = 0;
     if (nbytes) CF_CUDA_Q(cudaMemcpyAsync(struct_out, d_structs, nbytes, cudaMemcpyDeviceToHost, st));

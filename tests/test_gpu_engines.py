@@ -1,0 +1,26 @@
+"""Several engines in one process.  A kernel's dynamic shared-memory limit is
+an attribute of the function, shared by every engine: an engine that needs
+little must not lower the limit another engine's launches rely on."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_engines_do_not_lower_each_others_shared_memory(P):
+    from contrafold_gpu_gb300.engine import Batch, Engine
+    rng = np.random.default_rng(51)
+    seqs = ["".join(rng.choice(list("ACGU"), size=330)) for _ in range(16)]
+    big = Batch(seqs)
+    a = Engine(P)
+    a.set_schedule("queue")
+    a.set_group(64)                  # 64 seats of 330 nt: above the 48 KB default
+    want = a.mea(big, 6.0)
+    b = Engine(P)                    # a second engine with small launches only
+    assert len(b.mea(Batch(["GGGGAAAACCCC"]), 6.0)[0]) == 12
+    assert a.mea(big, 6.0) == want   # engine a's large launch still goes through
+    a.set_schedule("group")
+    a.set_group(0)
+    assert a.mea(big, 6.0) == want
+    a.close()
+    b.close()
