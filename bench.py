@@ -699,7 +699,7 @@ def side_arm(args):
         B = Batch(seqs)
         res = {}
         with ClockSampler(0) as clk:
-            for sched in ("auto", "queue", "warp", "group"):
+            for sched in ("auto", "warp", "group"):
                 eng = Engine(P)
                 eng.set_schedule(sched)
                 for w in range(args.warmup):

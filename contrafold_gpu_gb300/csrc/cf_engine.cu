@@ -192,10 +192,10 @@ int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err)
                 r.jobs |= 1u << k;   // the Job enum's order
             }
         }
-        static const char* scheds[] = {"warp", "cta", "group", "cluster", "queue"};
+        static const char* scheds[] = {"warp", "cta", "group", "cluster"};
         int k = 0;
-        while (k < 5 && f[6] != scheds[k]) ++k;
-        if (k == 5) { err = "line " + std::to_string(ln) + ": unknown schedule '" + f[6] + "'"; return CF_EINVAL; }
+        while (k < 4 && f[6] != scheds[k]) ++k;
+        if (k == 4) { err = "line " + std::to_string(ln) + ": unknown schedule '" + f[6] + "'"; return CF_EINVAL; }
         r.sched = k + 1;
         rows.push_back(r);
     }
@@ -494,7 +494,6 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
     }
     for (int mode = 0; mode < 4; ++mode) ks.push_back(cf::warp_kernel(mode));
     for (int mode = 0; mode < 3; ++mode) ks.push_back(cf::cta_kernel(mode));
-    for (int mode = 0; mode < 4; ++mode) ks.push_back(cf::queue_kernel(mode));
     const cf::ClusterKernels ck = cf::cluster_kernels();
     for (cf::FoldKernel k : {ck.mea, ck.bpp, ck.inside_acc}) ks.push_back((const void*)k);
     for (const void* k : ks) {
@@ -973,7 +972,10 @@ int cf_engine_set_mode(cf_engine* e, int mode) {
 
 int cf_engine_set_schedule(cf_engine* e, int kind, int ctas_per_sm) {
     if (!e) return fail(CF_EINVAL, "engine is NULL");
-    if (kind < 0 || kind > 5 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
+    if (kind == 5)
+        return fail(CF_EINVAL, "the queue schedule (kind 5) is disabled: its kernel did not finish in two GPU test "
+                               "runs and stays off the GPU until the cause is found");
+    if (kind < 0 || kind > 4 || ctas_per_sm < 0) return fail(CF_EINVAL, "bad schedule");
     e->sched = kind;
     e->ctas_per_sm = ctas_per_sm;
     return CF_OK;

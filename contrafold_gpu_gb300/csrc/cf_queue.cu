@@ -1,6 +1,14 @@
 // cf_queue.cu -- the dataflow schedule: one persistent launch for batches of
 // any length mix, in which warps pull (sequence, step, chunk) work items.
 //
+// DISABLED: cf_engine_set_schedule refuses this schedule and the schedule
+// table does not accept it, so nothing launches this kernel.  In two GPU test
+// runs (the 1/3/64-seat MEA/BPP/logZ test and the sampling test) a launch did
+// not finish, although every wait below is bounded in time; the cause has not
+// been found.  It was also slower than the grouped kernels on every measured
+// batch (10,000 x 200 nt MEA 15.8k vs 33.4k folds/s; 4,096 x U{40..400} 12.4k
+// vs 16.3k).
+//
 // Every CTA keeps `seats` sequences in progress at once.  A sequence's fold
 // is a chain of steps -- inside diagonals (pipelined two-phase steps
 // A(t) + B(t-1)), the exterior recurrence, outside diagonals, the posterior,
@@ -65,6 +73,9 @@ struct QueueSmemHead {
 };
 
 constexpr int kQueueWarps = kQueueThreads / 32;
+#ifndef CF_QUEUE_MAX_BACKOFF_NS
+#define CF_QUEUE_MAX_BACKOFF_NS 2048
+#endif
 constexpr unsigned long long kIdleLimitNs = 20ull * 1000 * 1000 * 1000;   // 20 s without any work: give up
 // a launch that is still scheduling after this long has lost its way: every
 // warp gives up at its next poll, with CF_ETIMEOUT
@@ -496,6 +507,7 @@ __global__ void __launch_bounds__(kQueueThreads, kQueueMinBlocks) k_fold_queue(Q
 
     int rot = warp;
     unsigned long long idle_since = 0;
+    unsigned backoff = 64;   // ns of sleep between polls, doubled while no work is found
     const unsigned long long t_start = globaltimer();
     for (;;) {
         if (globaltimer() - t_start > kLaunchLimitNs) {
@@ -529,10 +541,13 @@ __global__ void __launch_bounds__(kQueueThreads, kQueueMinBlocks) k_fold_queue(Q
                 if (lane == 0) atomicExch(A.status, CF_ETIMEOUT);
                 break;
             }
-            __nanosleep(200);
+            // back off while idle (a polling warp takes issue slots from working ones)
+            __nanosleep(backoff);
+            backoff = backoff < CF_QUEUE_MAX_BACKOFF_NS ? 2 * backoff : backoff;
             continue;
         }
         idle_since = 0;
+        backoff = 64;
         got_chunk = __shfl_sync(0xffffffffu, got_chunk, 0);
         got_gen = __shfl_sync(0xffffffffu, got_gen, 0);
         rot = got_seat;

@@ -189,14 +189,14 @@ class Engine:
 
     def set_schedule(self, kind: str = "auto", ctas_per_sm: int = 0):
         """Batched-path schedule: 'auto', 'warp', 'cta' (persistent, + residency cap), 'group',
-        'cluster' (each sequence folded by a thread-block cluster: latency of long sequences) or
-        'queue' (one persistent launch, warps pulling (sequence, step, chunk) items)."""
+        'cluster' (each sequence folded by a thread-block cluster: latency of long sequences);
+        'queue' is refused by the library (the queue schedule is disabled)."""
         self._check(self.lib.cf_engine_set_schedule(self._h, {"auto": 0, "warp": 1, "cta": 2, "group": 3,
                                                               "cluster": 4, "queue": 5}[kind],
                                                     int(ctas_per_sm)))
 
     def set_group(self, group: int = 0):
-        """Sequences per CTA of the grouped kernels (<= 32) or of the queue schedule (<= 64); 0 = automatic."""
+        """Sequences per CTA of the grouped kernels (<= 32; up to 64 accepted and capped); 0 = automatic."""
         self._check(self.lib.cf_engine_set_group(self._h, int(group)))
 
     def set_budget(self, nbytes: int):

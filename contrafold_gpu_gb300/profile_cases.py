@@ -10,7 +10,6 @@ enough that a full-section capture ends in a minute or two:
   viterbi  k_viterbi64: 1,216 x 200 nt drawn as the MEA workload
   sample   k_inside32acc + k_sample32: 1,024 sequences drawn as the sampling workload x 10 samples
   adj      k_adj_inside + k_adj_outside: 152 x 300 nt drawn as the gradient workload
-  queue    k_fold_queue<MEA>: 2,432 x 200 nt on the queue schedule, 2 seats per CTA
 """
 from __future__ import annotations
 
@@ -37,18 +36,12 @@ def run(case: str) -> None:
             s4, bonus = workloads.grad_300(152, 300)
             for _ in range(2):
                 grad.logz_grad(s4, None, list(bonus), engine=eng)
-        elif case == "queue":
-            eng.set_schedule("queue")
-            eng.set_group(2)
-            B = Batch(seqs, masks)
-            for _ in range(2):
-                eng.mea(B, 6.0)
         elif case == "group":
             B = Batch(seqs, masks)
             for _ in range(2):
                 eng.mea(B, 6.0)
         else:
-            raise SystemExit(f"unknown case {case!r}: group, viterbi, sample, adj or queue")
+            raise SystemExit(f"unknown case {case!r}: group, viterbi, sample or adj")
     finally:
         eng.close()
 

@@ -96,19 +96,15 @@ int cf_engine_set_mode(cf_engine* eng, int mode);
  * fused kernel, 3 = length-grouped per-phase kernels, 4 = cluster: each
  * sequence (or group, cf_engine_set_group) folded by the 8 CTAs of a
  * thread-block cluster on 8 SMs -- the latency of long sequences, for logZ,
- * BPP, MEA and sampling, 5 = queue: one persistent launch for any mix of
- * lengths, in which each CTA keeps several sequences ("seats",
- * cf_engine_set_group) in progress and its warps pull (sequence, step,
- * chunk) work items -- inside / outside diagonals, posterior, MEA
- * wavefront, samples -- refilling seats from a device queue of sequences,
- * for logZ, BPP, MEA and sampling (kind 0 follows the schedule table,
+ * BPP, MEA and sampling (kind 0 follows the schedule table,
  * cf_engine_load_tuning); ctas_per_sm caps the residency of the persistent
- * CTA and queue kernels (0 = automatic).  Results are identical for every
- * choice. */
+ * CTA kernels (0 = automatic).  Results are identical for every choice.
+ * Kind 5 (the queue schedule, cf_queue.cu) is disabled and returns
+ * CF_EINVAL: its kernel did not finish in two GPU test runs. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
-/* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32,
- * or of the queue schedule (kind 5, sequences in progress per CTA): 1..64;
- * 0 = automatic.  The tuner's knob; results are identical for every value. */
+/* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32
+ * (larger values are accepted and capped); 0 = automatic.  The tuner's knob;
+ * results are identical for every value. */
 int cf_engine_set_group(cf_engine* eng, int group);
 /* Schedule table of the automatic batched path (schedule kind 0), written by
  * the tuner (python -m contrafold_gpu_gb300.autotune --write-table FILE).
@@ -119,9 +115,9 @@ int cf_engine_set_group(cf_engine* eng, int group);
  * limit), its lengths are all within 25 % of each other (uniform = "uniform"),
  * or not ("mixed"), or either ("any"), and its job is in `jobs` ("all" or a
  * comma list of logz, logz64, bpp, mea, mfe, sample).  The first matching row
- * gives the schedule (warp, cta, group, cluster or queue), the sequences per
- * CTA of the grouped kernels or the queue's seats, and the CTAs per SM of
- * the CTA and queue kernels (0 = automatic);
+ * gives the schedule (warp, cta, group or cluster), the sequences per CTA of
+ * the grouped kernels, and the CTAs per SM of the CTA kernels (0 =
+ * automatic);
  * a batch no row matches folds grouped.  path NULL restores the built-in
  * table; cf_engine_create loads the file named by the environment variable
  * CONTRAFOLD_GB300_TUNING when it is set.  A malformed file is CF_EINVAL and
@@ -183,8 +179,9 @@ int cf_sample_seeded(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets
  * (gpu_contrafold/gpu.py:586-601): the tasks ordered by length (a stable
  * sort), cut into chunks of `chunk`, chunk c0 sampled with seed + c0 and its
  * k-th task with sequence index k -- the samples that cf_sample gives for
- * each chunk -- but every task folded in one submission (one persistent
- * launch on the queue schedule).  Task b writes L_b bytes at out[offsets[b]]. */
+ * each chunk -- but every task folded in one submission (the batched fold
+ * and sampler kernels over all tasks, each task's Philox key and sequence
+ * index given per task).  Task b writes L_b bytes at out[offsets[b]]. */
 int cf_sample_tasks(cf_engine* eng, const uint8_t* seqs, const int64_t* offsets,
                     const uint8_t* mask, int32_t n, int32_t chunk, uint64_t seed,
                     char* out);

@@ -10,11 +10,11 @@ pytestmark = pytest.mark.gpu
 def test_engines_do_not_lower_each_others_shared_memory(P):
     from contrafold_gpu_gb300.engine import Batch, Engine
     rng = np.random.default_rng(51)
-    seqs = ["".join(rng.choice(list("ACGU"), size=330)) for _ in range(16)]
+    seqs = ["".join(rng.choice(list("ACGU"), size=560)) for _ in range(32)]
     big = Batch(seqs)
     a = Engine(P)
-    a.set_schedule("queue")
-    a.set_group(64)                  # 64 seats of 330 nt: above the 48 KB default
+    a.set_schedule("group")
+    a.set_group(32)                  # the codes of 32 sequences of 560 nt in one CTA: above the 48 KB default
     want = a.mea(big, 6.0)
     b = Engine(P)                    # a second engine with small launches only
     assert len(b.mea(Batch(["GGGGAAAACCCC"]), 6.0)[0]) == 12

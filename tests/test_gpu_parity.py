@@ -18,11 +18,11 @@ from conftest import golden_post, mask_of
 pytestmark = pytest.mark.gpu
 
 
-PATHS = ["plain", "warp", "cta", "group", "cluster", "queue"]
+PATHS = ["plain", "warp", "cta", "group", "cluster"]
 
 
 def set_path(engine, path):
-    """plain = per-phase kernels, one sequence per CTA; warp / cta / queue =
+    """plain = per-phase kernels, one sequence per CTA; warp / cta =
     the persistent batched kernels; group / cluster = the grouped kernels on
     one CTA / on a thread-block cluster."""
     if path == "plain":
@@ -148,7 +148,7 @@ def test_plain_equals_batched(engine):
         res[path] = (engine.logz(B), engine.mea(B, 6.0), engine.mfe(B), z, np.concatenate([m.ravel() for m in mats]))
     set_path(engine, "cta")
     engine.set_schedule("auto")
-    for path in ("warp", "cta", "group", "cluster", "queue"):
+    for path in ("warp", "cta", "group", "cluster"):
         assert np.array_equal(res["plain"][0], res[path][0])
         assert res["plain"][1] == res[path][1]
         assert res["plain"][2] == res[path][2]
@@ -245,28 +245,13 @@ def test_long_sequence_cluster_vs_oracle(engine, P, oracle):
         assert a.tobytes() == b.tobytes()
 
 
-def test_queue_seats_and_slicing(engine, P, oracle):
-    """The queue schedule with 1, 3 and 64 seats per CTA and under a budget
-    that leaves room for a single CTA of seats: identical results."""
-    from contrafold_gpu_gb300.engine import Batch
-    seqs, masks = _rand_batch(71, 150, 1, 330, 0.1)
-    B = Batch(seqs, masks)
-    set_path(engine, "group")
-    mats_g, z_g = engine.bpp(B)
-    want = (engine.mea(B, 6.0), engine.logz(B).tobytes(), z_g.tobytes(),
-            hashlib.sha256(np.concatenate([m.ravel() for m in mats_g]).tobytes()).hexdigest())
-    set_path(engine, "queue")
-    try:
-        for seats in (1, 3, 64):
-            engine.set_group(seats)
-            mats, z = engine.bpp(B)
-            got = (engine.mea(B, 6.0), engine.logz(B).tobytes(), z.tobytes(),
-                   hashlib.sha256(np.concatenate([m.ravel() for m in mats]).tobytes()).hexdigest())
-            assert got == want, seats
-        engine.set_group(0)
-        engine.set_budget(40 << 20)
-        assert engine.mea(B, 6.0) == want[0]
-    finally:
-        engine.set_group(0)
-        engine.set_budget(0)
-    assert want[0] == oracle.batch(oracle.JOB_MEA, seqs, P, masks, 6.0)
+def test_queue_schedule_refused(engine, tmp_path):
+    """The queue schedule is disabled: the engine refuses it (no launch), and a
+    schedule table naming it is rejected."""
+    from contrafold_gpu_gb300.engine import EngineError
+    with pytest.raises(EngineError):
+        engine.set_schedule("queue")
+    t = tmp_path / "q.txt"
+    t.write_text("0 400 1 0 any all queue 0 0\n")
+    with pytest.raises(EngineError):
+        engine.load_tuning(str(t))

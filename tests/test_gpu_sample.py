@@ -84,25 +84,6 @@ def test_sample_frequencies_random_masked(engine, P, oracle):
     check_pair_frequencies(out, oracle.bpp_exact(seq, P, mask), n)
 
 
-def test_sample_queue_equals_grouped(engine):
-    """The queue schedule draws its samples inside the fold's own launch: the
-    same samples as the grouped inside + sampler kernel (same tables, same
-    Philox streams), with one seed for the batch and with a seed per sequence."""
-    from contrafold_gpu_gb300.engine import Batch
-    rng = np.random.default_rng(19)
-    seqs = ["".join(rng.choice(list("ACGU"), size=int(L))) for L in rng.integers(1, 420, 60)]
-    masks = [(rng.random(len(s)) < 0.1).astype(np.int8) if k % 2 else None for k, s in enumerate(seqs)]
-    B = Batch(seqs, masks)
-    out = {}
-    try:
-        for sched in ("group", "queue"):
-            engine.set_schedule(sched)
-            out[sched] = (engine.sample(B, 7, seed=99), engine.sample(B, 3, seeds=list(range(100, 160))))
-    finally:
-        engine.set_schedule("auto")
-    assert out["group"] == out["queue"]
-
-
 def test_fold_tasks_one_submission_equals_chunked(P):
     """fold_tasks_gpu submits every task at once; its samples equal the
     reference's chunked loop (tasks sorted by length, chunk c0 sampled with
