@@ -10,16 +10,24 @@
 // unpaired positions) -- a soft DMS/SHAPE constraint.  Counts come from the
 // inside/outside tables: every transition t of the recursion has probability
 // exp(outside(parent) + inside(children) + score(t) - logZ); the kernel below
-// enumerates all transitions and adds that probability, in FP64, to each
-// parameter-table entry the transition's score uses.  Inside and outside are
+// enumerates all transitions and adds that probability to each
+// parameter-table entry the transition's score uses.  P(k unpaired) is
+// 1 - sum over the pairs (k, x) of P(pair), and P(pair (i, j+1)) =
+// exp(FCo[i][j] + FC[i][j] - logZ).  Inside and outside are
 // evaluated with the accurate float32 log-sum-exp so the counts are the
 // derivative of the logZ that cf_logz reports (within float32 rounding).
 //
-// Kernels: one CTA per sequence, threads over the cells of a span (the shape
-// of the plain path).  k_adj_inside fills the inside tables; k_adj_outside
-// then walks the diagonals downwards, computing the outside values of
-// diagonal t and, in the same step, the transition probabilities of diagonal
-// t + 1 (whose outside values are final by then).
+// Kernels: one CTA per sequence, one warp per DP cell: the lanes split the
+// cell's candidate terms (the 496 single-branch window slots, the O(L)
+// bifurcation and outside chains) and combine their partial sums with a
+// fixed butterfly, so every cell costs a few warp iterations instead of one
+// thread's serial loop, and lanes never idle on a short diagonal.
+// k_adj_inside fills the inside tables; k_adj_outside then walks the
+// diagonals downwards, computing the outside values of diagonal t and, in the
+// same step, the transition probabilities of diagonal t + 1 (whose outside
+// values are final by then).  No result has a bitwise target (the reference
+// has no gradient), but every sum is taken in a fixed order, so results are
+// the same on every run.
 //
 // Memory.  The bifurcation and exterior terms read FC, FM, FM1 and the
 // outside FM2o at every span, so those four tables are kept whole.  FCo,
@@ -40,11 +48,25 @@
 namespace cf {
 namespace {
 
+constexpr int kWin = (CMAX + 1) * (CMAX + 2) / 2;   // single-branch window slots, l1 + l2 <= CMAX
+constexpr int kAdjWarps = kFoldThreads / 32;
+
 struct AdjSmem {
     SmemTabs<float> tabs;
     unsigned long long cnt_lo[CF_BLOB_LEN];   // fixed-point counts (x 2^62), low 64 bits
     unsigned cnt_hi[CF_BLOB_LEN];             // carries out of cnt_lo (units of 4)
+    unsigned char win_l1[kWin], win_l2[kWin]; // window slot -> (l1, l2), rows l1 ascending
 };
+
+__device__ __forceinline__ void load_window(AdjSmem* sm) {
+    for (int c = threadIdx.x; c < kWin; c += blockDim.x) {
+        // row l1 holds CMAX + 1 - l1 slots and starts at l1 (CMAX + 1) - l1 (l1 - 1) / 2
+        int l1 = 0, start = 0;
+        while (start + (CMAX + 1 - l1) <= c) start += CMAX + 1 - l1++;
+        sm->win_l1[c] = (unsigned char)l1;
+        sm->win_l2[c] = (unsigned char)(c - start);
+    }
+}
 
 // Cells of the FM2 checkpoints (diagonals 0, k, 2k, ... <= L) and the offset
 // of checkpoint c (diagonal c k, m - c k cells).
@@ -59,10 +81,10 @@ constexpr int kRingFM1o = 3;   // FM1o: spans t .. t + 2
 
 // Adjoint arena (4-byte words): FC FM FM1 (triangles), F5, F5o, FM2o
 // (triangle), the FCo / FMo / FM1o ring buffers, the FM2 checkpoints, the
-// FP64 bonus prefix U, and the fixed-point unpaired difference arrays (adds
-// at lo + 1 and subtractions at hi + 1, 128 bits each: two uint64).
+// FP64 bonus prefix U, and the fixed-point pairing probability of every
+// position (128 bits each: a low and a high uint64 array).
 struct ArenaAdj {
-    int64_t FC, FM, FM1, F5, F5o, FM2o, RC, RM, R1, FM2, U, UD, total;
+    int64_t FC, FM, FM1, F5, F5o, FM2o, RC, RM, R1, FM2, U, PD, total;
 };
 __host__ __device__ __forceinline__ ArenaAdj arena_adj(int L, int k) {
     ArenaAdj r;
@@ -73,8 +95,8 @@ __host__ __device__ __forceinline__ ArenaAdj arena_adj(int L, int k) {
     r.R1 = r.RM + kRingFMo * rw;
     r.FM2 = r.R1 + kRingFM1o * rw;
     r.U = r.FM2 + pad32(ckpt_cells(L, k));
-    r.UD = r.U + 2 * v;                 // doubles
-    r.total = r.UD + 8 * v;             // 4 x uint64[L + 2]
+    r.PD = r.U + 2 * v;                 // doubles
+    r.total = r.PD + 4 * v;             // 2 x uint64[L + 2]
     return r;
 }
 
@@ -89,7 +111,7 @@ struct AdjView {
     float* R1;        // FM1o ring
     float* FM2;       // checkpoints
     const double* U;  // U[k] = sum_{t<=k} u_t
-    unsigned long long* UD;   // [4][L + 2]: add lo, add hi, sub lo, sub hi
+    unsigned long long* PD;   // [2][L + 2]: P(position paired), low and high words
     int m, rw, k, L;
     __device__ __forceinline__ float& fco(int a, int t) const { return RC[(t % kRingFCo) * rw + a]; }
     __device__ __forceinline__ float& fmo(int a, int t) const { return RM[(t % kRingFMo) * rw + a]; }
@@ -109,7 +131,7 @@ __device__ __forceinline__ AdjView adj_view(const FoldArgs& A, const SeqDesc& D,
     V.RC = base + r.RC; V.RM = base + r.RM; V.R1 = base + r.R1;
     V.FM2 = base + r.FM2;
     V.U = reinterpret_cast<const double*>(base + r.U);
-    V.UD = reinterpret_cast<unsigned long long*>(base + r.UD);
+    V.PD = reinterpret_cast<unsigned long long*>(base + r.PD);
     V.m = D.L + 1;
     V.rw = (int)pad32(D.L + 1);
     V.k = k;
@@ -124,6 +146,7 @@ __device__ __forceinline__ float ubon(const double* U, int k) { return (float)(U
 __device__ __forceinline__ SeqView adj_setup(AdjSmem* sm, const FoldArgs& A, SeqDesc& D) {
     D = A.descs[blockIdx.x];
     load_tabs(&sm->tabs, A.blob32);
+    load_window(sm);
     int8_t* s = reinterpret_cast<int8_t*>(sm + 1);
     const int stride = (D.L + 2 + 15) & ~15;
     int8_t* pc = s + stride;
@@ -149,15 +172,34 @@ __device__ __forceinline__ float single_e(const ParamView<float>& P, const SmemT
 }
 
 
-// FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j], k ascending, live terms only.
-__device__ __forceinline__ float fm2_chain(const LseAcc32& sr, const InTabs<float>& T, int i, int j) {
+// Log-sum-exp of the 32 lanes' partial sums by a fixed butterfly; every lane
+// gets the same value (LseAcc32's plus is symmetric in its arguments).
+__device__ __forceinline__ float warp_lse(float x) {
+    const LseAcc32 sr{};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = sr.plus(x, __shfl_xor_sync(0xffffffffu, x, o));
+    return x;
+}
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// FM2[i][j] = (+)_{i<k<j} FM1[i][k] * FM[k][j], live terms only; lane l takes
+// k = i + 1 + l, i + 33 + l, ...  Called by a whole warp; the inside and the
+// recomputation in the outside use this one function, so a recomputed FM2 is
+// bitwise the stored one.
+__device__ __forceinline__ float fm2_warp(const InTabs<float>& T, int i, int j, int lane) {
+    const LseAcc32 sr{};
     float fm2 = CF_NEG32;
-    for (int k = i + 1; k < j; ++k) {
+    for (int k = i + 1 + lane; k < j; k += 32) {
         const float a = T.FM1[T.at(i, k)], b = T.FM[T.at(k, j)];
         if (a > CF_HALF32 && b > CF_HALF32) fm2 = sr.plus(fm2, __fadd_rn(a, b));
     }
-    return fm2;
+    return warp_lse(fm2);
 }
+
 
 }  // namespace
 
@@ -186,40 +228,40 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const f
     }
     __syncthreads();
     const InTabs<float>& T = V.I;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int d = 0; d <= L; ++d) {
         const bool keep = d % ckpt == 0;
         float* fm2_ck = V.FM2 + (keep ? ckpt_off(d / ckpt, m, ckpt) : 0);
-        for (int i = threadIdx.x; i + d <= L; i += blockDim.x) {
+        for (int i = warp; i + d <= L; i += kAdjWarps) {   // one warp per cell
             const int j = i + d, at = tri_off(d, m) + i;
             const bool fm_region = (0 < i) && (i + 2 <= j) && (j < L);
             const bool fc_cell = (0 < i) && (j < L) && Q.pairable(i, j + 1);
-            const float fm2 = fm_region ? fm2_chain(sr, T, i, j) : CF_NEG32;
-            if (keep) fm2_ck[i] = fm2;
+            const float fm2 = fm_region ? fm2_warp(T, i, j, lane) : CF_NEG32;
             float fc = CF_NEG32;
             if (fc_cell) {
                 const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
+                // single-branch candidates: window slot c = (l1, l2), inner pair (p+1, q)
+                float part = CF_NEG32;
+                for (int c = lane; c < kWin; c += 32) {
+                    const int l1 = sm->win_l1[c], l2 = sm->win_l2[c];
+                    if (l1 + l2 > d - 2) continue;   // q >= p + 2
+                    const int p = i + l1, q = j - l2;
+                    if (!Q.pairable(p + 1, q)) continue;
+                    const float inner = T.FC[T.at(p + 1, q - 1)];
+                    if (!(inner > CF_HALF32)) continue;
+                    const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
+                    const float b = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
+                    part = sr.plus(part, __fadd_rn(__fadd_rn(e, inner), b));
+                }
                 const float jB = sm->tabs.jB[idx4(si, sj1, si1, sj)];
                 float acc = __fadd_rn(__fadd_rn(jB, P.hp(d <= DHP ? d : DHP)), bon(V.U, i, j));
-                const int pmax = (i + CMAX < j) ? i + CMAX : j;
-                for (int p = i; p <= pmax; ++p) {
-                    int qmin = p + 2;
-                    if (p - i + j - CMAX > qmin) qmin = p - i + j - CMAX;
-                    for (int q = j; q >= qmin; --q) {
-                        if (!Q.pairable(p + 1, q)) continue;
-                        const float inner = T.FC[T.at(p + 1, q - 1)];
-                        if (!(inner > CF_HALF32)) continue;
-                        const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
-                        const float b = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
-                        acc = sr.plus(acc, __fadd_rn(__fadd_rn(e, inner), b));
-                    }
-                }
+                acc = sr.plus(acc, warp_lse(part));
                 if (fm2 > CF_HALF32) {
                     const float jA = junctionA<LseAcc32>(P, L, Q, i, j);
                     acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(fm2, jA), P.mp()), P.mb()));
                 }
                 fc = acc;
             }
-            T.FC[at] = fc;
             float fm1 = CF_NEG32, fm = CF_NEG32;
             if (fm_region) {
                 float acc = CF_NEG32;
@@ -238,8 +280,12 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_inside(FoldArgs A, const f
                 if (fm1 > CF_HALF32) acc = sr.plus(acc, fm1);
                 fm = acc;
             }
-            T.FM1[at] = fm1;
-            T.FM[at] = fm;
+            if (lane == 0) {
+                if (keep) fm2_ck[i] = fm2;
+                T.FC[at] = fc;
+                T.FM1[at] = fm1;
+                T.FM[at] = fm;
+            }
         }
         __syncthreads();
     }
@@ -298,14 +344,13 @@ __device__ __forceinline__ void add128g(unsigned long long* lo, unsigned long lo
 
 struct Counter {
     AdjSmem* sm;
-    unsigned long long* ud;   // global [4][L + 2]: add lo, add hi, sub lo, sub hi
+    unsigned long long* pd;   // global [2][L + 2]: P(position paired), low and high words
     int n;                    // L + 2
     __device__ __forceinline__ void add(int e, unsigned long long v) const { add128(&sm->cnt_lo[e], &sm->cnt_hi[e], v); }
-    // positions (lo, hi] unpaired with probability v
-    __device__ __forceinline__ void unp(int lo, int hi, unsigned long long v) const {
-        if (hi <= lo) return;
-        add128g(ud + lo + 1, ud + n + lo + 1, v);
-        add128g(ud + 2 * n + hi + 1, ud + 3 * n + hi + 1, v);
+    // positions a and b paired with each other with probability v
+    __device__ __forceinline__ void pair(int a, int b, unsigned long long v) const {
+        add128g(pd + a, pd + n + a, v);
+        add128g(pd + b, pd + n + b, v);
     }
 };
 
@@ -329,35 +374,50 @@ __device__ __forceinline__ void count_jB(const Counter& C, int sa, int sb1, int 
 }
 
 // Outside values of cell (a, b), span t, into the ring slots of diagonal t.
+// Called by a whole warp; lane 0 writes.
 __device__ __forceinline__ void outside_cell(const AdjSmem* sm, const ParamView<float>& P, const SeqView& Q,
-                                             const AdjView& V, int a, int b) {
+                                             const AdjView& V, int a, int b, int lane) {
     const LseAcc32 sr{};
     const int L = V.L, t = b - a;
     const InTabs<float>& I = V.I;
     const bool fm_region = (0 < a) && (a + 2 <= b) && (b < L);
     float fmo = CF_NEG32, fm1o = CF_NEG32;
     if (fm_region) {
-        float acc = CF_NEG32;
-        for (int i = 1; i < a; ++i) {
+        // FMo[a][b]: multiloop FM2o[i][b] * FM1[i][a] over i < a, and the extension
+        float part = CF_NEG32;
+        for (int i = 1 + lane; i < a; i += 32) {
             const float src = V.fm2o(i, b), f1 = I.FM1[I.at(i, a)];
-            if (src > CF_HALF32 && f1 > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, f1));
+            if (src > CF_HALF32 && f1 > CF_HALF32) part = sr.plus(part, __fadd_rn(src, f1));
         }
+        float acc = warp_lse(part);
         if (b + 1 < L) acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.fmo(a, t + 1), P.mu()), ubon(V.U, b + 1)));
         fmo = acc;
-        acc = CF_NEG32;
-        if (a >= 2) acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.fm1o(a - 1, t + 1), P.mu()), ubon(V.U, a)));
-        for (int j = b + 1; j < L; ++j) {
+        // FM1o[a][b]: FM2o[a][j] * FM[b][j] over j > b, the extension, and FMo
+        part = CF_NEG32;
+        for (int j = b + 1 + lane; j < L; j += 32) {
             const float src = V.fm2o(a, j), fmk = I.FM[I.at(b, j)];
-            if (src > CF_HALF32 && fmk > CF_HALF32) acc = sr.plus(acc, __fadd_rn(src, fmk));
+            if (src > CF_HALF32 && fmk > CF_HALF32) part = sr.plus(part, __fadd_rn(src, fmk));
         }
+        acc = warp_lse(part);
+        if (a >= 2) acc = sr.plus(acc, __fadd_rn(__fadd_rn(V.fm1o(a - 1, t + 1), P.mu()), ubon(V.U, a)));
         fm1o = sr.plus(acc, fmo);
     }
-    V.fmo(a, t) = fmo;
-    V.fm1o(a, t) = fm1o;
     float fco = CF_NEG32;
     if (0 < a && b < L && Q.pairable(a, b + 1)) {
         const int sa = Q.s[a], sb1 = Q.s[b + 1];
-        float acc = CF_NEG32;
+        // the pair (a, b+1) as the inner pair of a single-branch loop closed by
+        // (i, j+1) = (a-1-l1, b+2+l2)
+        float part = CF_NEG32;
+        for (int c = lane; c < kWin; c += 32) {
+            const int i = a - 1 - sm->win_l1[c], j = b + 1 + sm->win_l2[c];
+            if (i < 1 || j >= L || !Q.pairable(i, j + 1)) continue;
+            const float src = V.fco(i, j - i);
+            if (!(src > CF_HALF32)) continue;
+            const float e = single_e(P, &sm->tabs, Q, i, j, a - 1, b + 1);
+            const float bb = __fadd_rn(bon(V.U, i, a - 1), bon(V.U, b + 1, j));
+            part = sr.plus(part, __fadd_rn(__fadd_rn(src, e), bb));
+        }
+        float acc = warp_lse(part);
         const float f5k = I.F5[a - 1];
         if (f5k > CF_HALF32) {
             const float jA = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
@@ -367,36 +427,27 @@ __device__ __forceinline__ void outside_cell(const AdjSmem* sm, const ParamView<
             const float jAji = junctionA_rev<LseAcc32>(P, L, Q, a - 1, b + 1);
             acc = sr.plus(acc, __fadd_rn(__fadd_rn(__fadd_rn(V.fm1o(a - 1, t + 2), jAji), P.mp()), P.bp(sa, sb1)));
         }
-        for (int l1 = 0; l1 <= CMAX; ++l1) {
-            const int i = a - 1 - l1;
-            if (i < 1) break;
-            for (int l2 = 0; l1 + l2 <= CMAX; ++l2) {
-                const int j = b + 1 + l2;
-                if (j >= L) break;
-                if (!Q.pairable(i, j + 1)) continue;
-                const float src = V.fco(i, j - i);
-                if (!(src > CF_HALF32)) continue;
-                const float e = single_e(P, &sm->tabs, Q, i, j, a - 1, b + 1);
-                const float bb = __fadd_rn(bon(V.U, i, a - 1), bon(V.U, b + 1, j));
-                acc = sr.plus(acc, __fadd_rn(__fadd_rn(src, e), bb));
-            }
-        }
         fco = acc;
     }
-    V.fco(a, t) = fco;
     float fm2o = CF_NEG32;
     if (fm_region) fm2o = sr.plus(fm2o, fmo);
     if (fco > CF_HALF32) {
         const float jA = junctionA<LseAcc32>(P, L, Q, a, b);
         fm2o = sr.plus(fm2o, __fadd_rn(__fadd_rn(__fadd_rn(fco, jA), P.mp()), P.mb()));
     }
-    V.fm2o(a, b) = fm2o;
+    if (lane == 0) {
+        V.fmo(a, t) = fmo;
+        V.fm1o(a, t) = fm1o;
+        V.fco(a, t) = fco;
+        V.fm2o(a, b) = fm2o;
+    }
 }
 
 // Transitions out of the states of cell (i, j) (its outside values final).
+// Called by a whole warp: the lanes split the single-branch window; lane 0
+// counts the cell's other transitions.
 __device__ __forceinline__ void count_cell(const AdjSmem* sm, const ParamView<float>& P, const SeqView& Q,
-                                           const AdjView& V, const Counter& C, float Z, int i, int j) {
-    const LseAcc32 sr{};
+                                           const AdjView& V, const Counter& C, float Z, int i, int j, int lane) {
     const int L = V.L, d = j - i, m = V.m;
     const InTabs<float>& I = V.I;
     auto prob = [&](float x) { return fixp(expf(__fsub_rn(x, Z))); };
@@ -406,61 +457,60 @@ __device__ __forceinline__ void count_cell(const AdjSmem* sm, const ParamView<fl
         if (fco > CF_HALF32) {
             const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
             const float jB = sm->tabs.jB[idx4(si, sj1, si1, sj)];
-            // hairpin
-            {
+            // single-branch loops: window slot c = (l1, l2), inner pair (p+1, q)
+            unsigned long long outer_jB = 0;
+            for (int c = lane; c < kWin; c += 32) {
+                const int l1 = sm->win_l1[c], l2 = sm->win_l2[c];
+                if (l1 + l2 > d - 2) continue;
+                const int p = i + l1, q = j - l2;
+                if (!Q.pairable(p + 1, q)) continue;
+                const float inner = I.FC[I.at(p + 1, q - 1)];
+                if (!(inner > CF_HALF32)) continue;
+                const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
+                const float bb = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
+                const unsigned long long v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(e, inner), bb)));
+                if (l1 == 0 && l2 == 0) {
+                    C.add(CF_OFF_BP + si1 * 5 + sj, v);
+                    C.add(CF_OFF_STACK + idx4(si, sj1, si1, sj), v);
+                } else {
+                    const int sa = Q.s[p + 1], sq = Q.s[q];
+                    C.add(CF_OFF_CS + l1 * 31 + l2, v);
+                    C.add(CF_OFF_BP + sa * 5 + sq, v);
+                    outer_jB += v;
+                    count_jB(C, sq, sa, Q.s[q + 1], Q.s[p], v);
+                    if (l1 == 0 && l2 == 1) C.add(CF_OFF_B01 + sj, v);
+                    else if (l1 == 1 && l2 == 0) C.add(CF_OFF_B01 + si1, v);
+                    else if (l1 == 1 && l2 == 1) C.add(CF_OFF_I11 + si1 * 5 + sj, v);
+                }
+            }
+            // the probabilities of the loops closed by one pair sum to at most
+            // P(pair) <= 1, so the warp's total fits 64 bits
+            outer_jB = warp_sum(outer_jB);
+            // multiloop closed by (i, j+1): FM2 from its checkpoint, or recomputed (whole warp)
+            float fm2 = CF_NEG32;
+            if (fm_region) fm2 = d % V.k == 0 ? V.FM2[ckpt_off(d / V.k, m, V.k) + i] : fm2_warp(I, i, j, lane);
+            if (lane == 0) {
+                if (outer_jB != 0) count_jB(C, si, sj1, si1, sj, outer_jB);
+                // the pair (i, j+1) itself
+                const float fc = I.FC[I.at(i, j)];
+                if (fc > CF_HALF32) C.pair(i, j + 1, prob(__fadd_rn(fco, fc)));
+                // hairpin
                 const int hl = d <= DHP ? d : DHP;
                 const unsigned long long v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(jB, P.hp(hl)), bon(V.U, i, j))));
                 count_jB(C, si, sj1, si1, sj, v);
                 C.add(CF_OFF_HPCUM + hl, v);
-                C.unp(i, j, v);
-            }
-            // single-branch loops
-            unsigned long long outer_jB = 0;
-            const int pmax = (i + CMAX < j) ? i + CMAX : j;
-            for (int p = i; p <= pmax; ++p) {
-                int qmin = p + 2;
-                if (p - i + j - CMAX > qmin) qmin = p - i + j - CMAX;
-                for (int q = j; q >= qmin; --q) {
-                    if (!Q.pairable(p + 1, q)) continue;
-                    const float inner = I.FC[I.at(p + 1, q - 1)];
-                    if (!(inner > CF_HALF32)) continue;
-                    const float e = single_e(P, &sm->tabs, Q, i, j, p, q);
-                    const float bb = __fadd_rn(bon(V.U, i, p), bon(V.U, q, j));
-                    const unsigned long long v = prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(e, inner), bb)));
-                    const int l1 = p - i, l2 = j - q;
-                    if (l1 == 0 && l2 == 0) {
-                        C.add(CF_OFF_BP + si1 * 5 + sj, v);
-                        C.add(CF_OFF_STACK + idx4(si, sj1, si1, sj), v);
-                    } else {
-                        const int sa = Q.s[p + 1], sq = Q.s[q];
-                        C.add(CF_OFF_CS + l1 * 31 + l2, v);
-                        C.add(CF_OFF_BP + sa * 5 + sq, v);
-                        outer_jB += v;
-                        count_jB(C, sq, sa, Q.s[q + 1], Q.s[p], v);
-                        if (l1 == 0 && l2 == 1) C.add(CF_OFF_B01 + sj, v);
-                        else if (l1 == 1 && l2 == 0) C.add(CF_OFF_B01 + si1, v);
-                        else if (l1 == 1 && l2 == 1) C.add(CF_OFF_I11 + si1 * 5 + sj, v);
-                    }
-                    C.unp(i, p, v);
-                    C.unp(q, j, v);
-                }
-            }
-            if (outer_jB != 0) count_jB(C, si, sj1, si1, sj, outer_jB);
-            // multiloop closed by (i, j+1): FM2 from its checkpoint, or recomputed
-            if (fm_region) {
-                const float fm2 = d % V.k == 0 ? V.FM2[ckpt_off(d / V.k, m, V.k) + i] : fm2_chain(sr, I, i, j);
                 if (fm2 > CF_HALF32) {
                     const float jA = junctionA<LseAcc32>(P, L, Q, i, j);
-                    const unsigned long long v =
+                    const unsigned long long w =
                         prob(__fadd_rn(fco, __fadd_rn(__fadd_rn(__fadd_rn(fm2, jA), P.mp()), P.mb())));
-                    count_jA(C, Q, L, i, j, v);
-                    C.add(CF_OFF_MP, v);
-                    C.add(CF_OFF_MB, v);
+                    count_jA(C, Q, L, i, j, w);
+                    C.add(CF_OFF_MP, w);
+                    C.add(CF_OFF_MB, w);
                 }
             }
         }
     }
-    if (fm_region) {
+    if (fm_region && lane == 0) {
         const float fm1o = V.fm1o(i, d);
         if (fm1o > CF_HALF32) {
             const float fin = I.FC[I.at(i + 1, j - 1)];
@@ -476,7 +526,6 @@ __device__ __forceinline__ void count_cell(const AdjSmem* sm, const ParamView<fl
             if (ext > CF_HALF32) {
                 const unsigned long long v = prob(__fadd_rn(fm1o, __fadd_rn(__fadd_rn(ext, P.mu()), ubon(V.U, i + 1))));
                 C.add(CF_OFF_MU, v);
-                C.unp(i, i + 1, v);
             }
         }
         const float fmo = V.fmo(i, d);
@@ -484,7 +533,6 @@ __device__ __forceinline__ void count_cell(const AdjSmem* sm, const ParamView<fl
         if (fmo > CF_HALF32 && prev > CF_HALF32) {
             const unsigned long long v = prob(__fadd_rn(fmo, __fadd_rn(__fadd_rn(prev, P.mu()), ubon(V.U, j))));
             C.add(CF_OFF_MU, v);
-            C.unp(j - 1, j, v);
         }
     }
 }
@@ -511,7 +559,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
         sm->cnt_lo[e] = 0ull;
         sm->cnt_hi[e] = 0u;
     }
-    for (int k = threadIdx.x; k < 4 * (L + 2); k += blockDim.x) V.UD[k] = 0ull;
+    for (int k = threadIdx.x; k < 2 * (L + 2); k += blockDim.x) V.PD[k] = 0ull;
     // exterior outside F5o (one warp)
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
@@ -544,15 +592,16 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
         }
     }
     __syncthreads();
-    const Counter C{sm, V.UD, L + 2};
+    const Counter C{sm, V.PD, L + 2};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float Z = I.F5[L];
     // step t: outside values of diagonal t, counts of diagonal t + 1 (final since the last step)
     for (int t = L; t >= -1; --t) {
         const int no = t >= 0 ? L + 1 - t : 0;
         const int nc = t + 1 <= L ? L - t : 0;
-        for (int c = threadIdx.x; c < no + nc; c += blockDim.x) {
-            if (c < no) outside_cell(sm, P, Q, V, c, c + t);
-            else count_cell(sm, P, Q, V, C, Z, c - no, c - no + t + 1);
+        for (int c = warp; c < no + nc; c += kAdjWarps) {   // one warp per cell
+            if (c < no) outside_cell(sm, P, Q, V, c, c + t, lane);
+            else count_cell(sm, P, Q, V, C, Z, c - no, c - no + t + 1, lane);
         }
         __syncthreads();
     }
@@ -564,7 +613,6 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
             const unsigned long long v =
                 fixp(expf(__fsub_rn(__fadd_rn(f5o, __fadd_rn(__fadd_rn(I.F5[j - 1], P.eu()), ubon(V.U, j))), Z)));
             C.add(CF_OFF_EU, v);
-            C.unp(j - 1, j, v);
         }
         for (int k = 0; k < j; ++k) {
             if (!Q.pairable(k + 1, j)) continue;
@@ -582,23 +630,16 @@ __global__ void __launch_bounds__(kFoldThreads) k_adj_outside(FoldArgs A, const 
     __syncthreads();
     double* out = counts_out + (int64_t)D.idx * CF_BLOB_LEN;
     for (int e = threadIdx.x; e < CF_BLOB_LEN; e += blockDim.x) out[e] = fixp_value((double)sm->cnt_hi[e], sm->cnt_lo[e]);
-    if (threadIdx.x == 0) {
-        // running 128-bit prefix of (adds - subtractions): P(k unpaired), exact, then rounded once
-        const int n = L + 2;
-        unsigned long long lo = 0ull;
-        long long hi = 0;
-        for (int k = 1; k <= L; ++k) {
-            const unsigned long long al = V.UD[k], sl = V.UD[2 * n + k];
-            const long long ah = (long long)V.UD[n + k], sh = (long long)V.UD[3 * n + k];
-            const unsigned long long lo1 = lo + al;
-            hi += ah + (lo1 < lo ? 1 : 0);
-            const unsigned long long lo2 = lo1 - sl;
-            hi -= sh + (lo2 > lo1 ? 1 : 0);
-            lo = lo2;
-            unpaired_out[D.seq_off + k - 1] = fixp_value((double)hi, lo);
-        }
-        if (A.logz) A.logz[D.idx] = Z;
+    // P(k unpaired) = 1 - P(k paired): 2^62 minus the 128-bit sum, exact, then rounded once
+    const int n = L + 2;
+    for (int k = 1 + threadIdx.x; k <= L; k += blockDim.x) {
+        const unsigned long long pl = V.PD[k], one = 1ull << 62;
+        const long long ph = (long long)V.PD[n + k];
+        const unsigned long long lo = one - pl;
+        const long long hi = -ph - (pl > one ? 1 : 0);
+        unpaired_out[D.seq_off + k - 1] = fixp_value((double)hi, lo);
     }
+    if (threadIdx.x == 0 && A.logz) A.logz[D.idx] = Z;
 }
 
 size_t adj_smem_bytes(int Lmax) { return sizeof(AdjSmem) + 2 * (size_t)((Lmax + 2 + 15) & ~15); }
