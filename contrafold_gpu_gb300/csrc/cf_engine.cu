@@ -48,21 +48,23 @@ int fail(int code, const std::string& msg) {
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
-    size_t cap = 0;   // elements
-    // Grows geometrically (at least doubling): cudaFree waits for the whole
-    // device, so a buffer that is re-sized on every larger batch would stall
-    // every other stream (the serving loop runs several engines at once).
+    size_t cap = 0;                     // elements
+    const cudaStream_t* sp = nullptr;   // set: stream-ordered (re)allocation on *sp
+    // Grows geometrically (at least doubling).  An engine's buffers are
+    // (re)allocated in stream order on the engine's stream (cudaMallocAsync /
+    // cudaFreeAsync from the device's memory pool): cudaFree waits for the
+    // whole device, and in the serving loop one worker's growing buffer held
+    // the others' batches back for seconds while the rest of the device kept
+    // working.  Buffers without a stream (plans) use cudaMalloc / cudaFree.
     int ensure(size_t n) {
         if (n <= cap) return CF_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
+        release();
         size_t want = std::max<size_t>(std::max<size_t>(n, 1), 2 * cap);
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        cudaError_t e = alloc(want);
         if (e == cudaErrorMemoryAllocation && want > std::max<size_t>(n, 1)) {   // no room to double
             cudaGetLastError();
             want = std::max<size_t>(n, 1);
-            e = cudaMalloc(&p, want * sizeof(T));
+            e = alloc(want);
         }
         if (e != cudaSuccess) {
             p = nullptr;
@@ -71,8 +73,17 @@ struct DevBuf {
         cap = want;
         return CF_OK;
     }
+    cudaError_t alloc(size_t elems) {
+        void* q = nullptr;
+        const cudaError_t e = sp ? cudaMallocAsync(&q, elems * sizeof(T), *sp) : cudaMalloc(&q, elems * sizeof(T));
+        p = static_cast<T*>(q);
+        return e;
+    }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (sp) cudaFreeAsync(p, *sp);
+            else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
     }
@@ -217,7 +228,9 @@ const TuneRow* match_tuning(const std::vector<TuneRow>& rows, Job job, int n, in
 
 struct cf_engine {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // the stream of the engine's calls: one of the two below
+    cudaStream_t stream_lo = nullptr;    // the device's default (lowest) priority
+    cudaStream_t stream_hi = nullptr;    // its highest priority (created on first use)
     DevBuf<float> blob32;
     DevBuf<double> blob64;
     DevBuf<float> arena;
@@ -234,6 +247,13 @@ struct cf_engine {
     DevBuf<int32_t> stream_idx;
     DevBuf<float> bonus;
     DevBuf<double> counts, unpaired;
+    // stream-ordered allocation of every buffer above on the engine's stream
+    void bind_buffers() {
+        const cudaStream_t* s = &stream;
+        blob32.sp = s; blob64.sp = s; arena.sp = s; seqs.sp = s; mask.sp = s; descs.sp = s; logz.sp = s;
+        logz64.sp = s; structs.sp = s; post.sp = s; post_offs.sp = s; status.sp = s; samples.sp = s; seeds.sp = s;
+        stream_idx.sp = s; bonus.sp = s; counts.sp = s; unpaired.sp = s;
+    }
     size_t budget = 0;   // bytes; 0 = automatic (half of free memory at first use)
     int mode = 1;        // 0 plain, 1 batched
     int sched = 0;       // batched schedule: 0 auto, 1 warp-persistent, 2 CTA-persistent, 3 grouped, 4 cluster
@@ -913,9 +933,27 @@ int cf_engine_create(const float* params32, const double* params64, int device, 
     CF_CUDA(cudaSetDevice(device));
     cf_engine* e = new cf_engine();
     e->device = device;
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&e->stream_lo, cudaStreamNonBlocking) != cudaSuccess) {
         delete e;
         return fail(CF_ECUDA, "cudaStreamCreate failed");
+    }
+    e->stream = e->stream_lo;
+    e->bind_buffers();
+    {
+        // freed blocks stay in the device's pool (no unmapping at each
+        // synchronisation), so a buffer's regrowth maps no new memory
+        static std::mutex pool_mu;
+        static std::vector<int> pool_set;
+        std::lock_guard<std::mutex> lk(pool_mu);
+        if (std::find(pool_set.begin(), pool_set.end(), device) == pool_set.end()) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            cudaGetLastError();
+            pool_set.push_back(device);
+        }
     }
     int rc = cf_engine_set_params(e, params32, params64);
     if (!rc) {
@@ -934,14 +972,34 @@ int cf_engine_create(const float* params32, const double* params64, int device, 
 int cf_engine_destroy(cf_engine* e) {
     if (!e) return CF_OK;
     cudaSetDevice(e->device);
-    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->stream_lo) cudaStreamSynchronize(e->stream_lo);
+    if (e->stream_hi) cudaStreamSynchronize(e->stream_hi);
     e->blob32.release(); e->blob64.release(); e->arena.release(); e->seqs.release(); e->mask.release();
     e->descs.release(); e->logz.release(); e->logz64.release(); e->structs.release(); e->post.release();
     e->post_offs.release(); e->status.release(); e->samples.release(); e->seeds.release(); e->stream_idx.release();
     e->bonus.release(); e->counts.release(); e->unpaired.release();
+    if (e->stream) cudaStreamSynchronize(e->stream);   // the stream-ordered frees
 
-    if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->stream_lo) cudaStreamDestroy(e->stream_lo);
+    if (e->stream_hi) cudaStreamDestroy(e->stream_hi);
     delete e;
+    return CF_OK;
+}
+
+int cf_engine_set_priority(cf_engine* e, int high) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    CF_CUDA(cudaSetDevice(e->device));
+    if (high && !e->stream_hi) {
+        int least = 0, greatest = 0;
+        CF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CF_CUDA(cudaStreamCreateWithPriority(&e->stream_hi, cudaStreamNonBlocking, greatest));
+    }
+    cudaStream_t next = high ? e->stream_hi : e->stream_lo;
+    if (next != e->stream) {
+        // the engine's calls are stream-ordered: finish the old stream's work first
+        CF_CUDA(cudaStreamSynchronize(e->stream));
+        e->stream = next;
+    }
     return CF_OK;
 }
 

@@ -21,11 +21,18 @@
 // Every result is what the same request gives alone: logZ and MEA do not
 // depend on batch composition, and samples use a per-request seed
 // (cf_sample_seeded).
+//
+// Tracing: with CONTRAFOLD_GB300_SERVER_TRACE=<file> set when the server is
+// created, every batch appends one line to <file>: worker, op, bucket,
+// requests, nucleotides, longest sequence, start and end (seconds since the
+// server was created), status.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -100,6 +107,10 @@ struct cf_server {
     double busy_s = 0;                   // summed batch wall time over workers
     double wait_s = 0, max_wait_s = 0;   // queue wait (submit -> batch start) over requests
     double serve_s = 0, max_serve_s = 0; // batch run time seen by each request
+    // batch trace (CONTRAFOLD_GB300_SERVER_TRACE)
+    FILE* trace = nullptr;
+    std::mutex trace_mu;
+    Clock::time_point t_created = Clock::now();
 
     int bucket_of(int32_t L) const {
         int b = 0;
@@ -178,6 +189,7 @@ void worker_loop(cf_server* S, int w) {
     std::vector<char> out;
     for (;;) {
         Key key{};
+        bool long_batch = false;
         {
             std::unique_lock<std::mutex> lk(S->mu);
             const bool may_long = w < S->long_workers;   // read under the lock: configure may change it
@@ -195,7 +207,7 @@ void worker_loop(cf_server* S, int w) {
                         best = it;
                 }
             if (best == S->queues.end()) continue;
-            const bool long_batch = S->is_long(best->first.bucket);
+            long_batch = S->is_long(best->first.bucket);
             key = best->first;
             auto& q = best->second;
             batch.clear();
@@ -227,8 +239,25 @@ void worker_loop(cf_server* S, int w) {
         }
         const auto t0 = Clock::now();
         for (Req* r : batch) r->t_start = t0;
+        // short batches at the device's highest stream priority: blocks of a
+        // long batch on another worker hold their SMs for hundreds of ms, and
+        // without priorities a steady stream of long launches kept short
+        // batches waiting for seconds
+        cf_engine_set_priority(eng, long_batch ? 0 : 1);
         run_batch(S, eng, key, batch, buf, offs, mask, seeds, lz, out);
         const auto t1 = Clock::now();
+        if (S->trace) {
+            int64_t nt = 0;
+            size_t lmax = 0;
+            for (Req* r : batch) {
+                nt += (int64_t)r->seq.size();
+                lmax = std::max(lmax, r->seq.size());
+            }
+            std::lock_guard<std::mutex> lk(S->trace_mu);
+            std::fprintf(S->trace, "%d %d %d %zu %lld %zu %.6f %.6f %d\n", w, key.op, key.bucket, batch.size(),
+                         (long long)nt, lmax, std::chrono::duration<double>(t0 - S->t_created).count(),
+                         std::chrono::duration<double>(t1 - S->t_created).count(), batch.empty() ? 0 : batch[0]->status);
+        }
         {
             std::lock_guard<std::mutex> lk(S->mu);
             const double serve = std::chrono::duration<double>(t1 - t0).count();
@@ -340,6 +369,8 @@ int cf_server_create(const float* params32, const double* params64, int device, 
         }
         S->engines.push_back(e);
     }
+    if (const char* tp = std::getenv("CONTRAFOLD_GB300_SERVER_TRACE"))
+        if (*tp) S->trace = std::fopen(tp, "a");
     for (int w = 0; w < n_workers; ++w) S->workers.emplace_back(worker_loop, S, w);
     *out = S;
     return CF_OK;
@@ -381,6 +412,7 @@ int cf_server_destroy(cf_server* S) {
     S->cv_work.notify_all();
     for (auto& t : S->workers) t.join();
     for (cf_engine* e : S->engines) cf_engine_destroy(e);
+    if (S->trace) std::fclose(S->trace);
     delete S;
     return CF_OK;
 }

@@ -102,6 +102,14 @@ int cf_engine_set_mode(cf_engine* eng, int mode);
  * Kind 5 (the queue schedule, cf_queue.cu) is disabled and returns
  * CF_EINVAL: its kernel did not finish in two GPU test runs. */
 int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
+/* Scheduling priority of the engine's calls: 0 = the device's default
+ * (lowest) stream priority, nonzero = its highest.  As SMs free up, pending
+ * blocks of higher-priority streams are placed first (running blocks are not
+ * preempted).  The serving loop folds short requests at high priority so that
+ * batches of long sequences on other engines cannot hold them back.  Waits
+ * for the engine's earlier work when the priority changes.  No reference
+ * counterpart. */
+int cf_engine_set_priority(cf_engine* eng, int high);
 /* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32
  * (larger values are accepted and capped); 0 = automatic.  The tuner's knob;
  * results are identical for every value. */
