@@ -262,6 +262,7 @@ struct cf_engine {
     size_t smem_optin = 0;
     std::vector<TuneRow> tuning = default_tuning();   // schedule table of the automatic path
     int grad_ckpt = 0;   // FM2 checkpoint spacing of cf_grad (0 = automatic by the longest sequence)
+    bool shared = false; // the device is shared with other engines' launches: no wide CTAs, no clusters
 };
 
 namespace {
@@ -372,6 +373,9 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
             }
         }
     }
+    // on a shared device a cluster waits for 8 SMs of one GPC to be free at
+    // once; between other engines' steady launches that took seconds
+    if (eng->shared && sched == 4) sched = 3;
     P.cluster = batched && sched == 4 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
     if (P.cluster) P.group = eng->group > 0 ? std::min(cf::kMaxGroup, eng->group) : 1;
     P.queue = batched && sched == 5 && (job == JOB_LOGZ || job == JOB_BPP || job == JOB_MEA || job == JOB_SAMPLE);
@@ -724,7 +728,9 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
         // each diagonal, the latency of small batches of long sequences)
         int sms = 0;
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
-        const bool wide = grid <= sms;
+        // (not on a shared device: a 512-thread CTA waits for an SM with room
+        // for all of it, which other engines' smaller CTAs kept taking first)
+        const bool wide = grid <= sms && !eng->shared;
         const dim3 blkw(wide ? cf::kFoldThreadsWide : cf::kFoldThreads);
         const cf::FoldKernels fk = cf::fold_kernels(wide);
         const cf::FoldKernel k_in = fk.inside, k_inacc = fk.inside_acc, k_out = fk.outside, k_post = fk.posterior,
@@ -983,6 +989,12 @@ int cf_engine_destroy(cf_engine* e) {
     if (e->stream_lo) cudaStreamDestroy(e->stream_lo);
     if (e->stream_hi) cudaStreamDestroy(e->stream_hi);
     delete e;
+    return CF_OK;
+}
+
+int cf_engine_set_shared(cf_engine* e, int on) {
+    if (!e) return fail(CF_EINVAL, "engine is NULL");
+    e->shared = on != 0;
     return CF_OK;
 }
 

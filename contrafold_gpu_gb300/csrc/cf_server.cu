@@ -367,6 +367,7 @@ int cf_server_create(const float* params32, const double* params64, int device, 
             delete S;
             return fail(rc, msg);
         }
+        cf_engine_set_shared(e, 1);   // the workers' launches share the device
         S->engines.push_back(e);
     }
     if (const char* tp = std::getenv("CONTRAFOLD_GB300_SERVER_TRACE"))

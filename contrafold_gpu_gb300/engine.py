@@ -26,7 +26,8 @@ _STATUS = {1: "invalid argument", 2: "out of device memory / over budget", 3: "d
 
 # Exported symbols of include/contrafold_gb300.h
 SYMBOLS = ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_priority", "cf_engine_set_group", "cf_engine_load_tuning",
+           "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_priority", "cf_engine_set_shared",
+           "cf_engine_set_group", "cf_engine_load_tuning",
            "cf_engine_tuning_rows", "cf_engine_set_grad_checkpoint", "cf_grad_arena_bytes", "cf_last_error",
            "cf_version", "cf_logz", "cf_logz64", "cf_bpp",
            "cf_mea", "cf_mfe", "cf_sample", "cf_sample_seeded", "cf_sample_tasks", "cf_grad", "cf_plan_create", "cf_plan_destroy", "cf_plan_arena_bytes",
@@ -66,6 +67,7 @@ def load_library(path: str = LIB_PATH):
         L.cf_engine_set_mode.argtypes = [vp, ctypes.c_int]
         L.cf_engine_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.cf_engine_set_priority.argtypes = [vp, ctypes.c_int]
+        L.cf_engine_set_shared.argtypes = [vp, ctypes.c_int]
         L.cf_engine_set_group.argtypes = [vp, ctypes.c_int]
         L.cf_engine_load_tuning.argtypes = [vp, ctypes.c_char_p]
         L.cf_engine_tuning_rows.argtypes = [vp]
@@ -100,8 +102,8 @@ def load_library(path: str = LIB_PATH):
         L.cf_plan_schedule.argtypes = [vp]
         L.cf_plan_schedule.restype = ctypes.c_char_p
         for name in ("cf_engine_create", "cf_engine_destroy", "cf_engine_set_params", "cf_engine_set_budget",
-                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_priority", "cf_engine_set_group",
-                     "cf_engine_load_tuning", "cf_engine_tuning_rows", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
+                     "cf_engine_set_mode", "cf_engine_set_schedule", "cf_engine_set_priority", "cf_engine_set_shared",
+                     "cf_engine_set_group", "cf_engine_load_tuning", "cf_engine_tuning_rows", "cf_logz", "cf_logz64", "cf_bpp", "cf_mea", "cf_mfe", "cf_sample",
                      "cf_sample_seeded", "cf_sample_tasks", "cf_plan_create", "cf_plan_destroy", "cf_plan_run", "cf_plan_status", "cf_plan_set_timing",
                      "cf_plan_phase_ms", "cf_plan_launches", "cf_plan_group", "cf_plan_set_graph"):
             getattr(L, name).restype = ctypes.c_int
@@ -199,6 +201,10 @@ class Engine:
     def set_priority(self, high: bool):
         """Fold at the device's highest stream priority (True) or its default (False)."""
         self._check(self.lib.cf_engine_set_priority(self._h, int(bool(high))))
+
+    def set_shared(self, on: bool):
+        """The device is shared with other engines' launches: no 512-thread CTAs, no clusters."""
+        self._check(self.lib.cf_engine_set_shared(self._h, int(bool(on))))
 
     def set_group(self, group: int = 0):
         """Sequences per CTA of the grouped kernels (<= 32; up to 64 accepted and capped); 0 = automatic."""

@@ -110,6 +110,13 @@ int cf_engine_set_schedule(cf_engine* eng, int kind, int ctas_per_sm);
  * for the engine's earlier work when the priority changes.  No reference
  * counterpart. */
 int cf_engine_set_priority(cf_engine* eng, int high);
+/* on != 0: the device runs other engines' launches at the same time (the
+ * serving loop's workers).  The engine then launches no 512-thread CTAs and
+ * no thread-block clusters (the cluster schedule folds grouped instead):
+ * such a launch waits until a whole SM, or 8 SMs of one GPC, have room at
+ * once, and between other engines' steady launches of smaller CTAs that took
+ * seconds.  Results are identical.  No reference counterpart. */
+int cf_engine_set_shared(cf_engine* eng, int on);
 /* Sequences per CTA of the length-grouped kernels (schedule kind 3): 1..32
  * (larger values are accepted and capped); 0 = automatic.  The tuner's knob;
  * results are identical for every value. */

@@ -24,3 +24,24 @@ def test_engines_do_not_lower_each_others_shared_memory(P):
     assert a.mea(big, 6.0) == want
     a.close()
     b.close()
+
+
+def test_shared_device_and_priority_keep_results(P):
+    """An engine in shared-device mode (no 512-thread CTAs, no clusters) and at
+    either stream priority folds exactly what the default engine folds."""
+    from contrafold_gpu_gb300.engine import Batch, Engine
+    rng = np.random.default_rng(52)
+    seqs = ["".join(rng.choice(list("ACGU"), size=int(L))) for L in (520, 560, 600, 150)]
+    masks = [(rng.random(len(s)) < 0.1).astype(np.int8) for s in seqs]
+    eng = Engine(P)
+    try:
+        for B in (Batch(seqs[:3], masks[:3]), Batch(seqs, masks)):   # all >= 512 nt (cluster row), and mixed
+            want = (eng.mea(B, 6.0), eng.logz(B).tobytes(), eng.sample(B, 5, seed=3))
+            eng.set_shared(True)
+            for high in (True, False, True):
+                eng.set_priority(high)
+                assert (eng.mea(B, 6.0), eng.logz(B).tobytes(), eng.sample(B, 5, seed=3)) == want
+            eng.set_priority(False)
+            eng.set_shared(False)
+    finally:
+        eng.close()
