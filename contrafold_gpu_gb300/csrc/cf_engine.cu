@@ -328,7 +328,8 @@ int make_plan(cf_engine* eng, Job job, const int64_t* offsets, int n, Plan& P) {
         CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, eng->device));
         // resident CTAs per SM of the kernel that will run: the fused MEA kernel
         // is built for more than the other grouped kernels
-        const int slots = std::max(1, (job == JOB_MEA ? cf::kFoldMinBlocksMea : cf::kFoldMinBlocks) * sms);
+        const int slots =
+            std::max(1, (job == JOB_MEA && !eng->shared ? cf::kFoldMinBlocksMea : cf::kFoldMinBlocks) * sms);
         // whole waves: the fewest waves whose groups fit kMaxGroup sequences
         const int waves = std::max(1, (n + cf::kMaxGroup * slots - 1) / (cf::kMaxGroup * slots));
         const int wave_group = std::min(cf::kMaxGroup, std::max(1, (n + waves * slots - 1) / (waves * slots)));
@@ -513,7 +514,8 @@ int ensure_smem(cf_engine* eng, size_t bytes) {
                                    (const void*)cf::k_inside64, (const void*)cf::k_viterbi64};
     for (bool wide : {false, true}) {
         const cf::FoldKernels fk = cf::fold_kernels(wide);
-        for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea, fk.fused_mea, fk.fused_bpp})
+        for (cf::FoldKernel k : {fk.inside, fk.inside_acc, fk.outside, fk.posterior, fk.mea, fk.fused_mea, fk.fused_bpp,
+                                 fk.fused_mea_shared})
             ks.push_back((const void*)k);
     }
     for (int mode = 0; mode < 4; ++mode) ks.push_back(cf::warp_kernel(mode));
@@ -770,7 +772,9 @@ int run_device(cf_engine* eng, Job job, const Plan& P, Exec& X, const uint8_t* d
                     break;
                 }
                 if (X.timer == nullptr) {   // one launch for all phases; per-phase kernels when timing
-                    CF_PHASE(0, ((job == JOB_BPP ? fk.fused_bpp : fk.fused_mea)<<<grid, blkw, smem, st>>>(A)));
+                    const cf::FoldKernel fused = job == JOB_BPP ? fk.fused_bpp
+                                               : eng->shared ? fk.fused_mea_shared : fk.fused_mea;
+                    CF_PHASE(0, (fused<<<grid, blkw, smem, st>>>(A)));
                     break;
                 }
                 CF_PHASE(0, (k_in<<<grid, blkw, smem, st>>>(Ai)));

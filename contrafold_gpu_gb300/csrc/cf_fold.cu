@@ -497,7 +497,10 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? kFoldMinBlocks : 1) k
 // ---------------------------------------------------------------------------
 // Fused grouped fold: one launch runs inside -> outside -> posterior -> MEA
 // decode (MODE 0) or posterior into the caller's matrices (MODE 1) for the
-// CTA's group.  Each CTA goes on to its next phase as soon as its own group
+// CTA's group.  MODE 2 is MODE 0 built for the register budget of the other
+// fold kernels (kFoldMinBlocks per SM instead of kFoldMinBlocksMea): on a
+// device shared with them, a CTA of any of them fits the slot another frees
+// (an 80-register CTA never fits where a 64-register one left).  Each CTA goes on to its next phase as soon as its own group
 // is done, instead of every phase waiting for the slowest CTA of the grid.
 // ---------------------------------------------------------------------------
 template <int NT, int MODE>
@@ -509,7 +512,7 @@ __global__ void __launch_bounds__(NT, NT == kFoldThreads ? (MODE == 0 ? kFoldMin
     inside_group<Lse32>(sm, A);
     outside_group(sm, A);
     __syncthreads();
-    if constexpr (MODE == 0) {
+    if constexpr (MODE == 0 || MODE == 2) {
         FoldArgs Ap = A;
         Ap.post_out = nullptr;
         Ap.logz = nullptr;
@@ -787,6 +790,7 @@ template __global__ void k_mea32<kFoldThreadsWide>(FoldArgs);
 
 template __global__ void k_fold_group32<kFoldThreads, 0>(FoldArgs);
 template __global__ void k_fold_group32<kFoldThreads, 1>(FoldArgs);
+template __global__ void k_fold_group32<kFoldThreads, 2>(FoldArgs);
 template __global__ void k_fold_group32<kFoldThreadsWide, 0>(FoldArgs);
 template __global__ void k_fold_group32<kFoldThreadsWide, 1>(FoldArgs);
 
@@ -794,10 +798,11 @@ FoldKernels fold_kernels(bool wide) {
     if (wide)
         return {k_inside32<kFoldThreadsWide>, k_inside32acc<kFoldThreadsWide>, k_outside32<kFoldThreadsWide>,
                 k_posterior32<kFoldThreadsWide>, k_mea32<kFoldThreadsWide>,
-                k_fold_group32<kFoldThreadsWide, 0>, k_fold_group32<kFoldThreadsWide, 1>};
+                k_fold_group32<kFoldThreadsWide, 0>, k_fold_group32<kFoldThreadsWide, 1>,
+                k_fold_group32<kFoldThreads, 2>};
     return {k_inside32<kFoldThreads>, k_inside32acc<kFoldThreads>, k_outside32<kFoldThreads>,
             k_posterior32<kFoldThreads>, k_mea32<kFoldThreads>,
-            k_fold_group32<kFoldThreads, 0>, k_fold_group32<kFoldThreads, 1>};
+            k_fold_group32<kFoldThreads, 0>, k_fold_group32<kFoldThreads, 1>, k_fold_group32<kFoldThreads, 2>};
 }
 
 ClusterKernels cluster_kernels() {

@@ -49,6 +49,7 @@ using FoldKernel = void (*)(FoldArgs);
 struct FoldKernels {
     FoldKernel inside, inside_acc, outside, posterior, mea;
     FoldKernel fused_mea, fused_bpp;   // k_fold_group32: all phases of MEA / BPP in one launch
+    FoldKernel fused_mea_shared;       // fused MEA at the other kernels' register budget (shared device)
 };
 FoldKernels fold_kernels(bool wide);
 // k_fold_cluster32: one group folded by the kClusterCtas CTAs of a cluster

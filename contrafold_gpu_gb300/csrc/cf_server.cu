@@ -189,7 +189,6 @@ void worker_loop(cf_server* S, int w) {
     std::vector<char> out;
     for (;;) {
         Key key{};
-        bool long_batch = false;
         {
             std::unique_lock<std::mutex> lk(S->mu);
             const bool may_long = w < S->long_workers;   // read under the lock: configure may change it
@@ -207,7 +206,7 @@ void worker_loop(cf_server* S, int w) {
                         best = it;
                 }
             if (best == S->queues.end()) continue;
-            long_batch = S->is_long(best->first.bucket);
+            const bool long_batch = S->is_long(best->first.bucket);
             key = best->first;
             auto& q = best->second;
             batch.clear();
@@ -239,11 +238,6 @@ void worker_loop(cf_server* S, int w) {
         }
         const auto t0 = Clock::now();
         for (Req* r : batch) r->t_start = t0;
-        // short batches at the device's highest stream priority: blocks of a
-        // long batch on another worker hold their SMs for hundreds of ms, and
-        // without priorities a steady stream of long launches kept short
-        // batches waiting for seconds
-        cf_engine_set_priority(eng, long_batch ? 0 : 1);
         run_batch(S, eng, key, batch, buf, offs, mask, seeds, lz, out);
         const auto t1 = Clock::now();
         if (S->trace) {
