@@ -5,6 +5,7 @@ usable, every call raises `EngineError`.
 """
 from __future__ import annotations
 
+import concurrent.futures as cfut
 import ctypes
 import os
 import threading
@@ -113,6 +114,21 @@ def load_library(path: str = LIB_PATH):
 
 def _p(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
+
+
+def _parallel_cast(x: np.ndarray, dtype: np.dtype) -> np.ndarray:
+    """x.astype(dtype), in chunks on up to 16 threads."""
+    out = np.empty(x.size, dtype)
+    n = x.size
+    k = max(1, min(16, os.cpu_count() or 1, n // (1 << 22)))
+    if k == 1:
+        np.copyto(out, x, casting="unsafe")
+        return out
+    edges = np.linspace(0, n, k + 1).astype(np.int64)
+    with cfut.ThreadPoolExecutor(k) as ex:
+        list(ex.map(lambda i: np.copyto(out[edges[i]:edges[i + 1]], x[edges[i]:edges[i + 1]], casting="unsafe"),
+                    range(k)))
+    return out
 
 
 class Batch:
@@ -250,8 +266,10 @@ class Engine:
             self._check(self.lib.cf_logz64(*self._args(B), _p(out, ctypes.c_double)))
         return out[:B.n]
 
-    def bpp(self, B: Batch):
-        """Returns (list of float32 (L, L) matrices, float32 logZ array)."""
+    def bpp(self, B: Batch, dtype=np.float32):
+        """Returns (list of (L, L) matrices, float32 logZ array).  The device
+        computes float32; dtype=np.float64 widens on the host, on several
+        threads (numpy releases the GIL in casts)."""
         sq = B.lens * B.lens
         po = np.zeros(B.n + 1, np.int64)
         np.cumsum(sq, out=po[1:])
@@ -260,6 +278,8 @@ class Engine:
         with self._lock:
             self._check(self.lib.cf_bpp(*self._args(B), _p(po, ctypes.c_int64), _p(post, ctypes.c_float),
                                         _p(z, ctypes.c_float)))
+        if np.dtype(dtype) != np.float32:
+            post = _parallel_cast(post, np.dtype(dtype))
         mats = [post[po[b]:po[b + 1]].reshape(int(B.lens[b]), int(B.lens[b])) for b in range(B.n)]
         return mats, z[:B.n]
 

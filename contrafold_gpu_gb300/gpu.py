@@ -90,5 +90,5 @@ def mfe_batch(seqs: Sequence[str], P: dict, forced_list=None) -> List[str]:
 def bpp_batch(seqs: Sequence[str], P: dict, forced_list=None) -> List[np.ndarray]:
     """Base-pair probability matrices (float64, (L, L), upper triangle) of a batch."""
     B = Batch(seqs, _masks(forced_list, len(seqs)))
-    mats, _ = engine_for(P).bpp(B)
-    return [m.astype(np.float64) for m in mats]
+    mats, _ = engine_for(P).bpp(B, np.float64)
+    return mats

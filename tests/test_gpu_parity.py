@@ -255,3 +255,17 @@ def test_queue_schedule_refused(engine, tmp_path):
     t.write_text("0 400 1 0 any all queue 0 0\n")
     with pytest.raises(EngineError):
         engine.load_tuning(str(t))
+
+
+def test_bpp_batch_float64(engine, P):
+    """gpu.bpp_batch returns float64 (L, L) matrices (the reference's bpp
+    dtype, cpu.py:929), each the device's float32 matrix widened exactly."""
+    from contrafold_gpu_gb300 import gpu
+    from contrafold_gpu_gb300.engine import Batch
+    seqs, masks = _rand_batch(81, 40, 1, 120, 0.1)
+    got = gpu.bpp_batch(seqs, P, masks)
+    want, _ = engine.bpp(Batch(seqs, masks))
+    assert len(got) == len(seqs)
+    for g, w, s in zip(got, want, seqs):
+        assert g.dtype == np.float64 and g.shape == (len(s), len(s))
+        assert np.array_equal(g, w.astype(np.float64))
