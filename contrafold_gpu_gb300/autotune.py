@@ -130,6 +130,25 @@ def time_mixed(P, n, Lmax, kind, reps=2):
     return n / best
 
 
+def time_sampling(P, n, Lmax, group, n_samples=100, reps=2):
+    """Samples/s of a mixed-length batch on the grouped schedule with `group`
+    sequences per CTA (0 = the engine's choice), fold included, host buffers."""
+    from .engine import Batch, Engine
+    seqs, _ = _mixed_batch(n, Lmax, 12)
+    B = Batch(seqs)
+    eng = Engine(P)
+    eng.set_schedule("group")
+    eng.set_group(group)
+    eng.sample(B, n_samples, seed=1)
+    best = float("inf")
+    for k in range(reps):
+        t0 = time.perf_counter()
+        eng.sample(B, n_samples, seed=2 + k)
+        best = min(best, time.perf_counter() - t0)
+    eng.close()
+    return n * n_samples / best
+
+
 def tuning_rows(P, lengths, batch_sizes, long_lengths, long_batches, log=print):
     """Measure and return the schedule table as text rows (first match wins)."""
     rows = ["# contrafold-gb300 schedule table, written by contrafold_gpu_gb300.autotune --write-table",
@@ -156,6 +175,15 @@ def tuning_rows(P, lengths, batch_sizes, long_lengths, long_batches, log=print):
         for n, best in sorted(cells, reverse=True):
             rows.append(f"0 {Lmax} {n} 0 mixed logz,bpp,mea {best} 0 0")
         prev = Lmax
+    # sampling of mixed lengths (the fold is an inside only): sequences per CTA
+    n = max(batch_sizes)
+    for Lmax in sorted(lengths):
+        rates = {g: time_sampling(P, n, Lmax, g) for g in (0, 2, 3, 4, 6)}
+        g = max(rates, key=rates.get)
+        log(f"sampling mixed <= {Lmax} nt n={n}: " + " ".join(f"g{k} {v / 1e6:.3f}M" for k, v in rates.items())
+            + f" -> {g}")
+        if g:
+            rows.append(f"0 {Lmax} {n} 0 mixed sample group {g} 0")
     return rows
 
 

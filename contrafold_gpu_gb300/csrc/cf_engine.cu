@@ -139,16 +139,21 @@ struct TuneRow {
 //  * large batches of mixed short lengths take the warp-per-sequence kernel
 //    (200 nt: n=1024 warp 8.7k vs grouped 10.2k MEA folds/s, n=2048 15.1k vs
 //    13.3k; 60 nt: n=2048 172k vs 186k, n=4096 238k vs 191k);
+//  * sampling of large mixed batches up to 400 nt folds 4 sequences per CTA
+//    (4,096 x U{40..400} x 100 samples: 1.30M samples/s against 1.20M with
+//    the MEA-tuned length table's 2);
 //  * everything else folds grouped (lengths within 25 %: one wave of full
 //    CTAs; mixed: several waves).
 std::vector<TuneRow> default_tuning() {
     const unsigned lbms = (1u << JOB_LOGZ) | (1u << JOB_BPP) | (1u << JOB_MEA) | (1u << JOB_SAMPLE);
     const unsigned lbm = (1u << JOB_LOGZ) | (1u << JOB_BPP) | (1u << JOB_MEA);
-    std::vector<TuneRow> t(4);
+    std::vector<TuneRow> t(5);
     t[0].min_len = 512; t[0].min_batch = 1; t[0].max_batch = 38; t[0].jobs = lbms; t[0].sched = 4;
     t[1].max_len = 80; t[1].min_batch = 4096; t[1].uniform = 0; t[1].jobs = lbm; t[1].sched = 1;
     t[2].max_len = 80; t[2].uniform = 0; t[2].jobs = lbm; t[2].sched = 3;
     t[3].max_len = 256; t[3].min_batch = 2048; t[3].uniform = 0; t[3].jobs = lbm; t[3].sched = 1;
+    t[4].max_len = 400; t[4].min_batch = 1024; t[4].uniform = 0; t[4].jobs = 1u << JOB_SAMPLE; t[4].sched = 3;
+    t[4].group = 4;
     return t;
 }
 

@@ -84,6 +84,26 @@ def test_sample_frequencies_random_masked(engine, P, oracle):
     check_pair_frequencies(out, oracle.bpp_exact(seq, P, mask), n)
 
 
+def test_sample_warp_schedule_equals_grouped(engine):
+    """The warp-persistent kernel draws every pick by evaluating all candidate
+    chunks twice; the grouped sampler (k_sample32) skips the chunks its first
+    pass recorded as unable to hold the pick.  Same tables, same Philox
+    streams: identical samples."""
+    from contrafold_gpu_gb300.engine import Batch
+    rng = np.random.default_rng(23)
+    seqs = ["".join(rng.choice(list("ACGU"), size=int(L))) for L in rng.integers(1, 300, 40)]
+    masks = [(rng.random(len(s)) < 0.1).astype(np.int8) if k % 3 == 0 else None for k, s in enumerate(seqs)]
+    B = Batch(seqs, masks)
+    out = {}
+    try:
+        for sched in ("group", "warp"):
+            engine.set_schedule(sched)
+            out[sched] = (engine.sample(B, 9, seed=31), engine.sample(B, 4, seeds=list(range(500, 540))))
+    finally:
+        engine.set_schedule("auto")
+    assert out["group"] == out["warp"]
+
+
 def test_fold_tasks_one_submission_equals_chunked(P):
     """fold_tasks_gpu submits every task at once; its samples equal the
     reference's chunked loop (tasks sorted by length, chunk c0 sampled with

@@ -28,7 +28,7 @@ def test_written_table_changes_schedule(P, tmp_path):
     from contrafold_gpu_gb300.engine import CF_JOB_LOGZ, CF_JOB_MEA, Engine
     eng = Engine(P)
     B = _batch(64, 120, 3)
-    assert eng.tuning_rows == 4
+    assert eng.tuning_rows == 5
     assert _schedule(eng, CF_JOB_MEA, B) == "group"          # built-in: uniform batches fold grouped
     want_mea, want_z = eng.mea(B, 6.0), eng.logz(B)
     t = tmp_path / "tuning.txt"
@@ -46,7 +46,7 @@ def test_written_table_changes_schedule(P, tmp_path):
     assert _schedule(eng, CF_JOB_MEA, B) == "group"
     eng.set_schedule("auto")
     eng.load_tuning(None)
-    assert eng.tuning_rows == 4 and _schedule(eng, CF_JOB_MEA, B) == "group"
+    assert eng.tuning_rows == 5 and _schedule(eng, CF_JOB_MEA, B) == "group"
     eng.close()
 
 
@@ -63,7 +63,7 @@ def test_malformed_table_rejected(P, tmp_path, text):
     t.write_text(text)
     with pytest.raises(EngineError):
         eng.load_tuning(str(t))
-    assert eng.tuning_rows == 4
+    assert eng.tuning_rows == 5
     with pytest.raises(EngineError):
         eng.load_tuning(str(tmp_path / "missing.txt"))
     eng.close()
