@@ -34,6 +34,13 @@ Bernoulli 0.1 / 0.3 on some, N on one) with the same fields as golden.json
     python tests/golden/make_golden.py --ref <reference checkout> --xlong
 writes tests/golden/xlong.json: one 800-nt and one 1,000-nt sequence (the
 latter with a Bernoulli 0.1 mask), about an hour of pure Python.
+
+    python tests/golden/make_golden.py --ref <reference checkout> --mea200 500
+writes tests/golden/mea200_subset.json.gz: the first 500 sequences of the
+10,000 x 200 nt MEA workload (contrafold_gpu_gb300.workloads.mea_200: bases
+default_rng(0), Bernoulli(0.1) mask default_rng(1)), each with FP64 logZ, the
+Viterbi and MEA (gamma 6) structures and the posterior digest (about half an
+hour of pure Python on 8 cores).
 """
 from __future__ import annotations
 
@@ -228,7 +235,28 @@ def main():
     ap.add_argument("--exhaustive", action="store_true", help="all short sequences (and masks): exhaustive.json.gz")
     ap.add_argument("--long", action="store_true", help="seven 300-600 nt sequences: long.json")
     ap.add_argument("--xlong", action="store_true", help="800 and 1,000 nt sequences: xlong.json")
+    ap.add_argument("--mea200", type=int, default=0, metavar="N",
+                    help="the first N sequences of the 200-nt MEA workload: mea200_subset.json.gz")
     args = ap.parse_args()
+    if args.mea200:
+        sys.path.insert(0, REPO)
+        from contrafold_gpu_gb300 import workloads
+        sb, mask = workloads.mea_200()
+        seqs = workloads.as_strings(sb)[:args.mea200]
+        masks = [m.astype(np.int8).tolist() for m in mask[:args.mea200]]
+        t0 = time.time()
+        with mp.get_context("spawn").Pool(args.jobs, initializer=_init, initargs=(args.ref,)) as pool:
+            rows = pool.map(_run_small, list(zip(seqs, masks)), chunksize=4)
+        out = args.out or os.path.join(HERE, "mea200_subset.json.gz")
+        doc = {"generator": f"tests/golden/make_golden.py --mea200 {args.mea200}",
+               "reference": "gpu_contrafold/cpu.py (pure Python under an identity numba.njit)",
+               "workload": "contrafold_gpu_gb300.workloads.mea_200(): first sequences, in order",
+               "seqs_sha256": hashlib.sha256("".join(seqs).encode()).hexdigest(),
+               "fields": ["seq", "mask", "logz64", "mfe", "mea_gamma6", "post_sha256_16"], "cases": rows}
+        with gzip.open(out, "wt") as fh:
+            json.dump(doc, fh, separators=(",", ":"))
+        print(f"wrote {len(rows)} cases to {out} in {time.time() - t0:.0f}s")
+        return
     if args.long or args.xlong:
         cases = long_cases() if args.long else xlong_cases()
         t0 = time.time()
