@@ -35,6 +35,13 @@ struct SmemFold {
 
 __host__ __device__ __forceinline__ int code_stride(int Lmax) { return (Lmax + 2 + 15) & ~15; }
 
+// Item index of this thread when one serial item per thread is dealt over the
+// warps first: thread (w, lane) takes item w + lane * warps.  A bijection of
+// [0, blockDim.x).
+__device__ __forceinline__ int tb_index() {
+    return (threadIdx.x >> 5) + (threadIdx.x & 31) * (int)(blockDim.x >> 5);
+}
+
 template <typename R>
 __device__ __forceinline__ unsigned char* dyn_smem(SmemFold<R>* sm) {
     return reinterpret_cast<unsigned char*>(sm + 1);
@@ -472,8 +479,11 @@ __device__ __forceinline__ void mea_group(SmemFold<float>* sm, const FoldArgs& A
         for (int t = tm.tid(); t < L; t += tm.nthreads()) out[t] = '.';
     }
     tm.sync();
+    // one traceback per thread, dealt over the warps first (lane 0 of every
+    // warp, then lane 1, ...): lanes of one warp with different tracebacks
+    // would run them one after another
     if (tm.rank() == 0)
-        for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
+        for (int g = tb_index(); g < sm->n; g += blockDim.x) {
             const int L = sm->L[g];
             const Arena32 ar = arena32(L);
             float* base = A.ws + sm->ws[g];
@@ -767,7 +777,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldMinBlocks) k_viterbi64(Fold
         for (int t = threadIdx.x; t < L; t += blockDim.x) out[t] = '.';
     }
     __syncthreads();
-    for (int g = threadIdx.x; g < sm->n; g += blockDim.x) {
+    for (int g = tb_index(); g < sm->n; g += blockDim.x) {   // tracebacks dealt over the warps first
         const SeqV Q = seq_v(sm, g);
         const InTabs<double> T = in_view<double>(A, sm->ws[g], Q.L).T;
         const Arena64 ar = arena64(Q.L);
