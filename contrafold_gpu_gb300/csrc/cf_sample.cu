@@ -12,11 +12,10 @@ struct SampleSmem {
     SmemTabs<float> tabs;
 };
 
-// Per-warp scratch: codes s[L+2], pc[L+2], packed stack[L+8], the picker's
-// chunk records.
+// Per-warp scratch: codes s[L+2], pc[L+2], packed stack[L+8].
 __host__ __device__ __forceinline__ int sample_region_bytes(int Lmax) {
     const int codes = ((Lmax + 2 + 15) & ~15) * 2;
-    return codes + 4 * (Lmax + 8) + 4 * 2 * kPickCache;
+    return codes + 4 * (Lmax + 8);
 }
 
 __global__ void __launch_bounds__(kSampleWarps * 32) k_sample32(SampleArgs A) {
@@ -31,7 +30,6 @@ __global__ void __launch_bounds__(kSampleWarps * 32) k_sample32(SampleArgs A) {
     int8_t* s = reinterpret_cast<int8_t*>(mine);
     int8_t* pc = s + cstride;
     uint32_t* stack = reinterpret_cast<uint32_t*>(mine + 2 * cstride);
-    float* pcache = reinterpret_cast<float*>(mine + 2 * cstride + 4 * (A.Lmax + 8));
     const int64_t n_items = (int64_t)A.n * A.n_samples;
     const int64_t gw = (int64_t)blockIdx.x * kSampleWarps + wib;
     const int64_t nw = (int64_t)gridDim.x * kSampleWarps;
@@ -64,10 +62,9 @@ __global__ void __launch_bounds__(kSampleWarps * 32) k_sample32(SampleArgs A) {
         const int sidx = A.stream_idx != nullptr ? A.stream_idx[D.idx] : (A.seeds != nullptr ? 0 : D.idx);
         if (A.seeds != nullptr) {
             const uint64_t sd = A.seeds[D.idx];
-            sample_one(X, smp, sidx, make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), out, stack, A.status, lane,
-                       pcache);
+            sample_one(X, smp, sidx, make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), out, stack, A.status, lane);
         } else {
-            sample_one(X, smp, sidx, key, out, stack, A.status, lane, pcache);
+            sample_one(X, smp, sidx, key, out, stack, A.status, lane);
         }
         __syncwarp();
     }

@@ -7,13 +7,7 @@
 // chunk with an inclusive warp scan; pass 2 repeats the identical scans and
 // stops at the first valid candidate whose running sum reaches r = U * S.
 // Because both passes add in the same order, the running sum of pass 2 ends
-// at exactly S >= r, so a pick always lands.  Pass 1 also records, per chunk
-// (up to kPickCache chunks, in a per-warp shared-memory cache), the chunk's
-// total and the largest running sum of its valid lanes; pass 2 then skips a
-// chunk without evaluating its candidates when run + that maximum < r -- no
-// lane of it could be picked (float addition with a fixed first operand is
-// monotone) -- adding the recorded total instead, which is the very value
-// pass 1 added.  The picks are exactly those of evaluating every chunk.  m is the state's own inside
+// at exactly S >= r, so a pick always lands.  m is the state's own inside
 // value (FC[i][j], FM[i][j], ...), which keeps the exponents near zero.
 // Candidate order and weights follow the reference: F5 (unpaired, then
 // k ascending), FC (hairpin, single-branch p ascending / q descending,
@@ -55,11 +49,8 @@ __device__ __forceinline__ float warp_scan(float x, int lane) {
     return x;
 }
 
-constexpr int kPickCache = 64;   // chunks whose totals pass 1 records (per warp: 2 x 64 floats)
-
-// Two-pass chunked pick.  An enumerator asks want() before it evaluates a
-// group of <= 32 candidates, then calls chunk(valid, w, payload) for it (both
-// warp-uniformly; chunk returns false to stop).
+// Two-pass chunked pick.  `enumerate(chunk)` calls chunk(valid, w, payload)
+// warp-uniformly for each group of <= 32 candidates (returns false to stop).
 struct Picker {
     int lane;
     float m;          // normaliser (the state's inside value)
@@ -67,16 +58,6 @@ struct Picker {
     float r;          // target (pass 2)
     bool pass2;
     int picked;       // payload of the pick, or INT32_MIN
-    float* cache;     // [2 * kPickCache]: per chunk (total, largest valid running sum); null: none
-    int nc;           // chunks seen
-    // false: pass 2 passes over this chunk (it cannot hold the pick)
-    __device__ __forceinline__ bool want() {
-        if (!pass2 || cache == nullptr || nc >= kPickCache) return true;
-        if (run + cache[2 * nc + 1] >= r) return true;
-        run += cache[2 * nc];
-        ++nc;
-        return false;
-    }
     __device__ __forceinline__ bool chunk(bool valid, float w, int payload) {
         const float x = valid ? expf(w - m) : 0.0f;
         const float inc = warp_scan(x, lane);
@@ -89,16 +70,8 @@ struct Picker {
                 picked = __shfl_sync(0xffffffffu, payload, t);
                 return false;
             }
-        } else if (cache != nullptr && nc < kPickCache) {
-            // non-negative floats order as their bit patterns
-            const int mx = __reduce_max_sync(0xffffffffu, valid ? __float_as_int(inc) : 0);
-            if (lane == 0) {
-                cache[2 * nc] = tot;
-                cache[2 * nc + 1] = __int_as_float(mx);
-            }
         }
         run += tot;
-        ++nc;
         return true;
     }
 };
@@ -115,13 +88,12 @@ template <class C, class QV>
 __device__ __forceinline__ void enum_f5(const SampleCtx<QV>& X, int j, int lane, C& ch) {
     const ParamView<float> P{X.tb->blob};
     const int L = X.Q.L;
-    if (ch.want()) {
+    {
         const float f = X.T.F5[j - 1];
         const bool v = lane == 0 && f > CF_HALF32;
         if (!ch.chunk(v, __fadd_rn(f, P.eu()), -1)) return;
     }
     for (int k0 = 0; k0 < j; k0 += 32) {
-        if (!ch.want()) continue;
         const int k = k0 + lane;
         bool v = false;
         float w = 0.0f;
@@ -145,7 +117,7 @@ __device__ __forceinline__ void enum_fc(const SampleCtx<QV>& X, int i, int j, in
     const int L = Q.L, d = j - i;
     const int si = Q.s[i], sj1 = Q.s[j + 1], si1 = Q.s[i + 1], sj = Q.s[j];
     const float jB = X.tb->jB[idx4(si, sj1, si1, sj)];
-    if (ch.want() && !ch.chunk(lane == 0, __fadd_rn(jB, P.hp(d <= DHP ? d : DHP)), 0)) return;
+    if (!ch.chunk(lane == 0, __fadd_rn(jB, P.hp(d <= DHP ? d : DHP)), 0)) return;
     const int pmax = (i + CMAX < j) ? i + CMAX : j;
     for (int p = i; p <= pmax; ++p) {
         const int l1 = p - i;
@@ -153,7 +125,6 @@ __device__ __forceinline__ void enum_fc(const SampleCtx<QV>& X, int i, int j, in
         if (l1 + j - CMAX > qmin) qmin = l1 + j - CMAX;
         const int cnt = j - qmin + 1;
         if (cnt <= 0) continue;
-        if (!ch.want()) continue;
         const int q = j - lane;
         bool v = false;
         float w = 0.0f;
@@ -180,7 +151,6 @@ __device__ __forceinline__ void enum_fc(const SampleCtx<QV>& X, int i, int j, in
     }
     const float jA = junctionA<Lse32>(P, L, Q, i, j);
     for (int k0 = i + 1; k0 < j; k0 += 32) {
-        if (!ch.want()) continue;
         const int k = k0 + lane;
         bool v = false;
         float w = 0.0f;
@@ -200,7 +170,6 @@ template <class C, class QV>
 __device__ __forceinline__ void enum_fm(const SampleCtx<QV>& X, int i, int j, int lane, C& ch) {
     const ParamView<float> P{X.tb->blob};
     for (int k0 = i + 1; k0 < j; k0 += 32) {
-        if (!ch.want()) continue;
         const int k = k0 + lane;
         bool v = false;
         float w = 0.0f;
@@ -210,14 +179,10 @@ __device__ __forceinline__ void enum_fm(const SampleCtx<QV>& X, int i, int j, in
         }
         if (!ch.chunk(v, w, k)) return;
     }
-    if (ch.want()) {
-        const float prev = X.T.FM[X.T.at(i, j - 1)];
-        if (!ch.chunk(lane == 0 && prev > CF_HALF32, __fadd_rn(prev, P.mu()), -1)) return;
-    }
-    if (ch.want()) {
-        const float f1 = X.T.FM1[X.T.at(i, j)];
-        ch.chunk(lane == 0 && f1 > CF_HALF32, f1, -2);
-    }
+    const float prev = X.T.FM[X.T.at(i, j - 1)];
+    if (!ch.chunk(lane == 0 && prev > CF_HALF32, __fadd_rn(prev, P.mu()), -1)) return;
+    const float f1 = X.T.FM1[X.T.at(i, j)];
+    ch.chunk(lane == 0 && f1 > CF_HALF32, f1, -2);
 }
 
 // FM1(i, j): payload 0 = pair (i+1, j), 1 = unpaired i+1
@@ -235,22 +200,18 @@ __device__ __forceinline__ void enum_fm1(const SampleCtx<QV>& X, int i, int j, i
             v = true;
         }
     }
-    if (ch.want() && !ch.chunk(lane == 0 && v, w, 0)) return;
-    if (ch.want()) {
-        const float ext = X.T.FM1[X.T.at(i + 1, j)];
-        ch.chunk(lane == 0 && ext > CF_HALF32, __fadd_rn(ext, P.mu()), 1);
-    }
+    if (!ch.chunk(lane == 0 && v, w, 0)) return;
+    const float ext = X.T.FM1[X.T.at(i + 1, j)];
+    ch.chunk(lane == 0 && ext > CF_HALF32, __fadd_rn(ext, P.mu()), 1);
 }
 
 template <class E>
-__device__ __forceinline__ int pick(E enumerate, float m, float u, int lane, int* status, float* cache) {
-    Picker pk{lane, m, 0.0f, 0.0f, false, INT32_MIN, cache, 0};
+__device__ __forceinline__ int pick(E enumerate, float m, float u, int lane, int* status) {
+    Picker pk{lane, m, 0.0f, 0.0f, false, INT32_MIN};
     enumerate(pk);
     const float S = pk.run;
-    __syncwarp();   // lane 0's chunk records
-    Picker p2{lane, m, 0.0f, u * S, true, INT32_MIN, cache, 0};
+    Picker p2{lane, m, 0.0f, u * S, true, INT32_MIN};
     enumerate(p2);
-    __syncwarp();   // the records are rewritten by the next pick
     if (p2.picked == INT32_MIN && lane == 0) atomicExch(status, CF_EDEVICE);
     return p2.picked;
 }
@@ -263,7 +224,7 @@ __device__ __forceinline__ int pick(E enumerate, float m, float u, int lane, int
 // interval of the sequence.
 template <class QV>
 __device__ __forceinline__ void sample_one(const SampleCtx<QV>& X, int smp, int seq_idx, uint2 key, char* out,
-                                           uint32_t* stack, int* status, int lane, float* pick_cache = nullptr) {
+                                           uint32_t* stack, int* status, int lane) {
     const int L = X.Q.L;
     uint32_t draw = 0;
     int sp = 0;
@@ -285,7 +246,7 @@ __device__ __forceinline__ void sample_one(const SampleCtx<QV>& X, int smp, int 
         const uint4 rnd = philox4x32_10(make_uint4((uint32_t)smp, draw++, (uint32_t)seq_idx, 0u), key);
         const float u = uniform01(rnd.x);
         if (typ == 0) {
-            const int pk = pick([&](auto& c) { enum_f5(X, j, lane, c); }, X.T.F5[j], u, lane, status, pick_cache);
+            const int pk = pick([&](auto& c) { enum_f5(X, j, lane, c); }, X.T.F5[j], u, lane, status);
             if (pk == INT32_MIN) break;
             if (pk == -1) {
                 push(0, 0, j - 1);
@@ -295,7 +256,7 @@ __device__ __forceinline__ void sample_one(const SampleCtx<QV>& X, int smp, int 
                 push(0, 0, pk);
             }
         } else if (typ == 1) {
-            const int pk = pick([&](auto& c) { enum_fc(X, i, j, lane, c); }, X.T.FC[X.T.at(i, j)], u, lane, status, pick_cache);
+            const int pk = pick([&](auto& c) { enum_fc(X, i, j, lane, c); }, X.T.FC[X.T.at(i, j)], u, lane, status);
             if (pk == INT32_MIN) break;
             if (pk >= 2048) {
                 const int k = pk - 2048;
@@ -308,7 +269,7 @@ __device__ __forceinline__ void sample_one(const SampleCtx<QV>& X, int smp, int 
                 push(1, p + 1, q - 1);
             }
         } else if (typ == 2) {
-            const int pk = pick([&](auto& c) { enum_fm(X, i, j, lane, c); }, X.T.FM[X.T.at(i, j)], u, lane, status, pick_cache);
+            const int pk = pick([&](auto& c) { enum_fm(X, i, j, lane, c); }, X.T.FM[X.T.at(i, j)], u, lane, status);
             if (pk == INT32_MIN) break;
             if (pk >= 0) {
                 push(3, i, pk);
@@ -319,7 +280,7 @@ __device__ __forceinline__ void sample_one(const SampleCtx<QV>& X, int smp, int 
                 push(3, i, j);
             }
         } else {
-            const int pk = pick([&](auto& c) { enum_fm1(X, i, j, lane, c); }, X.T.FM1[X.T.at(i, j)], u, lane, status, pick_cache);
+            const int pk = pick([&](auto& c) { enum_fm1(X, i, j, lane, c); }, X.T.FM1[X.T.at(i, j)], u, lane, status);
             if (pk == INT32_MIN) break;
             if (pk == 0) {
                 if (lane == 0) { out[i] = '('; out[j - 1] = ')'; }

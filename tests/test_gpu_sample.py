@@ -85,10 +85,9 @@ def test_sample_frequencies_random_masked(engine, P, oracle):
 
 
 def test_sample_warp_schedule_equals_grouped(engine):
-    """The warp-persistent kernel draws every pick by evaluating all candidate
-    chunks twice; the grouped sampler (k_sample32) skips the chunks its first
-    pass recorded as unable to hold the pick.  Same tables, same Philox
-    streams: identical samples."""
+    """The warp-persistent kernel (inside and samples in one launch) and the
+    grouped inside + k_sample32 draw identical samples: same tables bit for
+    bit, same Philox streams."""
     from contrafold_gpu_gb300.engine import Batch
     rng = np.random.default_rng(23)
     seqs = ["".join(rng.choice(list("ACGU"), size=int(L))) for L in rng.integers(1, 300, 40)]
