@@ -429,11 +429,12 @@ __device__ __forceinline__ void inside_B(const S& sr, const SmemTabs<typename S:
             const R jB2 = tb->jB[idx4(sq, sa, Q.s[q + 1], Q.s[p])];
             const R snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : R(0));
             e = S::add(S::add(S::add(P.cs(l1, l2), P.bp(sa, sq)), jB), jB2);
-            // the reference adds snuc = 0 too; the Viterbi (Max64, bound by the
-            // FP64 pipe) skips that add where snuc is 0 for the whole row: x + 0
-            // is x except that -0 becomes +0, which no comparison can see and
-            // later sums keep only in the sign of a zero
-            if (!(std::is_same<S, Max64>::value && l1 >= 2)) e = S::add(e, snuc);
+            // the reference adds snuc = 0 too; that add is skipped where snuc is 0
+            // for the whole row (l1 >= 2): x + 0 is x except that -0 becomes +0,
+            // which no comparison, log-sum-exp or max can see and later sums keep
+            // only in the sign of a zero (the Viterbi is bound by the FP64 pipe:
+            // one add of six per candidate)
+            if (l1 < 2) e = S::add(e, snuc);
         }
         acc = sr.plus(acc, S::add(e, v));
     };

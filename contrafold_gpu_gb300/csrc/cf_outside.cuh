@@ -263,8 +263,8 @@ __device__ __forceinline__ void outside_B(const Lse32& sr, const SmemTabs<float>
             e = __fadd_rn(P.bp(si1, sj), P.stack(si, Q.s[j + 1], si1, sj));
         } else {
             const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
-            const float snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f);
-            e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), bp_ab), jBij), jB2), snuc);
+            e = __fadd_rn(__fadd_rn(__fadd_rn(P.cs(l1, l2), bp_ab), jBij), jB2);
+            if (l1 < 2) e = __fadd_rn(e, l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f));   // + 0 skipped (see inside_B)
         }
         acc = sr.plus(acc, __fadd_rn(v, e));
     };
@@ -383,8 +383,8 @@ __device__ __forceinline__ float posterior_pair(const SmemTabs<float>* __restric
             e = __fadd_rn(__fadd_rn(__fadd_rn(outside, P.bp(si1, sj)), P.stack(si, Q.s[j + 1], si1, sj)), fcin);
         } else {
             const float jBij = tb->jB[idx4(si, Q.s[j + 1], si1, sj)];
-            const float snuc = l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f);
-            e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l1, l2)), fcin), bp_ab), jB2), snuc);
+            e = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(outside, jBij), P.cs(l1, l2)), fcin), bp_ab), jB2);
+            if (l1 < 2) e = __fadd_rn(e, l2 == 0 ? sn0 : (l2 == 1 ? sn1 : 0.0f));   // + 0 skipped (see inside_B)
         }
         post = __fadd_rn(post, fexp32(pt, e));
     };
