@@ -63,6 +63,39 @@ def test_batch_packing_and_masks():
     assert Batch(["AC"], [None]).mask is None
 
 
+def test_batch_mask_types_match_per_sequence_packing():
+    """Masks as lists, int8 / bool / uint8 arrays, 2-D rows and None, with
+    nonzero values other than 1: the packed bytes equal a per-sequence copy
+    of (mask != 0)."""
+    from contrafold_gpu_gb300.engine import Batch
+    rng = np.random.default_rng(5)
+    lens = [int(x) for x in rng.integers(0, 40, 60)]
+    seqs = ["".join(rng.choice(list("ACGU"), size=L)) for L in lens]
+    masks = []
+    for k, L in enumerate(lens):
+        kind = k % 5
+        m = rng.integers(0, 3, L + (k % 3))            # some masks longer than their sequence
+        masks.append(None if kind == 0 else m.tolist() if kind == 1 else m.astype(np.int8) if kind == 2
+                     else (m != 0) if kind == 3 else m.astype(np.uint8).reshape(1, -1))
+    B = Batch(seqs, masks)
+    want = np.zeros(max(sum(lens), 1), np.uint8)
+    o = 0
+    for m, L in zip(masks, lens):
+        if m is not None:
+            want[o:o + L] = np.asarray(m).reshape(-1)[:L] != 0
+        o += L
+    assert B.mask.dtype == np.uint8 and np.array_equal(B.mask[:sum(lens)], want[:sum(lens)])
+
+
+def test_parallel_cast_equals_astype():
+    from contrafold_gpu_gb300.engine import _parallel_cast
+    rng = np.random.default_rng(6)
+    for n in (0, 1, 5, (1 << 22) + 3, 3 * (1 << 22) + 17):
+        x = rng.random(n, dtype=np.float32)
+        y = _parallel_cast(x, np.dtype(np.float64))
+        assert y.dtype == np.float64 and np.array_equal(y, x.astype(np.float64))
+
+
 def test_params_loader_tying(P):
     from contrafold_gpu_gb300 import params
     raw = params.read_raw()
