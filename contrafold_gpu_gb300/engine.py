@@ -116,6 +116,18 @@ def _p(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
 
 
+def _text_buffer(n: int):
+    """A zeroed host byte buffer of n bytes and the char* to pass (large
+    buffers come as untouched zero pages, so zeroing costs nothing up front)."""
+    arr = np.zeros(max(int(n), 1), np.uint8)
+    return arr, ctypes.cast(arr.ctypes.data, ctypes.c_char_p)
+
+
+def _text(arr: np.ndarray, n: int) -> str:
+    """The first n bytes of `arr` as ASCII text (one copy)."""
+    return str(memoryview(arr)[:int(n)], "ascii")
+
+
 def _parallel_cast(x: np.ndarray, dtype: np.dtype) -> np.ndarray:
     """x.astype(dtype), in chunks on up to 16 threads."""
     out = np.empty(x.size, dtype)
@@ -169,9 +181,10 @@ class Batch:
             mk = (mk != 0).view(np.uint8)
             self.mask = mk if mk.size else np.zeros(1, np.uint8)
 
-    def split_strings(self, raw: bytes, per: int = 1) -> List[str]:
-        s = raw.decode("ascii")
-        return [s[self.offsets[b] * per:self.offsets[b + 1] * per] for b in range(self.n)]
+    def split_strings(self, raw, per: int = 1) -> List[str]:
+        s = raw.decode("ascii") if isinstance(raw, (bytes, bytearray)) else raw
+        o = self.offsets.tolist()
+        return [s[o[b] * per:o[b + 1] * per] for b in range(self.n)]
 
 
 class Engine:
@@ -284,23 +297,23 @@ class Engine:
         return mats, z[:B.n]
 
     def mea(self, B: Batch, gamma: float = 6.0) -> List[str]:
-        out = ctypes.create_string_buffer(max(B.total, 1))
+        arr, out = _text_buffer(B.total)
         with self._lock:
             self._check(self.lib.cf_mea(*self._args(B), ctypes.c_float(float(np.float32(gamma))), out))
-        return B.split_strings(out.raw[:B.total])
+        return B.split_strings(_text(arr, B.total))
 
     def mfe(self, B: Batch) -> List[str]:
-        out = ctypes.create_string_buffer(max(B.total, 1))
+        arr, out = _text_buffer(B.total)
         with self._lock:
             self._check(self.lib.cf_mfe(*self._args(B), out))
-        return B.split_strings(out.raw[:B.total])
+        return B.split_strings(_text(arr, B.total))
 
     def sample(self, B: Batch, n_samples: int, seed: int = 0, seeds: Optional[Sequence[int]] = None) -> List[List[str]]:
         """Samples per sequence.  With `seeds` (one per sequence) sequence b draws
         what it draws alone with seed seeds[b] (cf_sample_seeded)."""
         if n_samples < 0:
             raise ValueError("n_samples must be >= 0")
-        out = ctypes.create_string_buffer(max(B.total * n_samples, 1))
+        arr, out = _text_buffer(B.total * n_samples)
         with self._lock:
             if seeds is None:
                 self._check(self.lib.cf_sample(*self._args(B), ctypes.c_int32(n_samples),
@@ -311,22 +324,27 @@ class Engine:
                     raise ValueError("one seed per sequence is required")
                 self._check(self.lib.cf_sample_seeded(*self._args(B), ctypes.c_int32(n_samples),
                                                       _p(sd, ctypes.c_uint64), out))
-        raw = out.raw[:B.total * n_samples].decode("ascii")
+        raw = _text(arr, B.total * n_samples)
         res = []
+        offs, lens = B.offsets.tolist(), B.lens.tolist()
         for b in range(B.n):
-            L = int(B.lens[b])
-            base = int(B.offsets[b]) * n_samples
-            res.append([raw[base + t * L: base + (t + 1) * L] for t in range(n_samples)])
+            L = lens[b]
+            if L == 0:
+                res.append([""] * n_samples)
+                continue
+            base = offs[b] * n_samples
+            chunk = raw[base:base + L * n_samples]   # this sequence's samples, one after another
+            res.append([chunk[i:i + L] for i in range(0, L * n_samples, L)])
         return res
 
     def sample_tasks(self, B: Batch, chunk: int = 4096, seed: int = 0) -> List[str]:
         """One sample per task with the chunk / seed semantics of the
         reference's fold_tasks_gpu, all tasks in one submission (cf_sample_tasks)."""
-        out = ctypes.create_string_buffer(max(B.total, 1))
+        arr, out = _text_buffer(B.total)
         with self._lock:
             self._check(self.lib.cf_sample_tasks(*self._args(B), ctypes.c_int32(int(chunk)),
                                                  ctypes.c_uint64(seed & 0xFFFFFFFFFFFFFFFF), out))
-        return B.split_strings(out.raw[:B.total])
+        return B.split_strings(_text(arr, B.total))
 
 
 def grad_arena_bytes(L: int, every: int = 0) -> int:
