@@ -86,3 +86,27 @@ def test_cancel_and_errors(P):
         with pytest.raises(ValueError):
             srv.submit(serve.Request("fold", "ACGU"))
         assert srv.stats()["cancelled"] == 1
+
+
+@pytest.mark.gpu
+def test_batch_trace(P, tmp_path, monkeypatch):
+    """CONTRAFOLD_GB300_SERVER_TRACE: one line per batch -- worker, op, bucket,
+    requests, nucleotides, longest sequence, start <= end, status -- covering
+    every request."""
+    trace = tmp_path / "trace.txt"
+    monkeypatch.setenv("CONTRAFOLD_GB300_SERVER_TRACE", str(trace))
+    reqs, _ = serve.mixed_workload(120, rate=1e9, seed=6, max_len=300)
+    with serve.Server(P, workers=2) as srv:
+        srv.pause(True)
+        tickets = [srv.submit(r) for r in reqs]
+        srv.pause(False)
+        for t in tickets:
+            srv.result(t)
+    rows = [line.split() for line in trace.read_text().splitlines()]
+    assert rows and all(len(r) == 9 for r in rows)
+    assert sum(int(r[3]) for r in rows) == len(reqs)
+    assert sum(int(r[4]) for r in rows) == sum(len(r.seq) for r in reqs)
+    for r in rows:
+        assert int(r[0]) in (0, 1) and int(r[1]) in (0, 1, 2) and int(r[8]) == 0
+        assert 0.0 <= float(r[6]) <= float(r[7])
+        assert 0 < int(r[5]) <= 300
