@@ -126,7 +126,7 @@ struct TuneRow {
     int min_batch = 0, max_batch = 0;        // n >= min_batch, n <= max_batch (0 = no limit)
     int uniform = -1;                        // 1: lengths within 25 %, 0: mixed, -1: either
     unsigned jobs = 0;                       // bit per Job (0 = every job)
-    int sched = 3;                           // 1 warp, 2 cta, 3 group, 4 cluster, 5 queue
+    int sched = 3;                           // 1 warp, 2 cta, 3 group, 4 cluster (5, queue: disabled)
     int group = 0;                           // sequences per CTA: grouped kernels / queue seats (0 = automatic)
     int ctas = 0;                            // resident CTAs per SM of the CTA kernel (0 = automatic)
 };
@@ -160,7 +160,8 @@ std::vector<TuneRow> default_tuning() {
 // Parses a schedule table: one row per line, '#' starts a comment,
 //   min_len max_len min_batch max_batch uniform jobs schedule group ctas_per_sm
 // uniform: any | uniform | mixed; jobs: all or a comma list of logz, logz64,
-// bpp, mea, mfe, sample; schedule: warp | cta | group | cluster | queue.
+// bpp, mea, mfe, sample; schedule: warp | cta | group | cluster (the disabled
+// queue schedule is rejected).
 int parse_tuning(std::istream& in, std::vector<TuneRow>& rows, std::string& err) {
     std::string line;
     int ln = 0;
@@ -288,7 +289,7 @@ struct Plan {
     bool cta = false;             // persistent CTA-per-sequence fused kernel (batched path)
     bool warp = false;            // persistent warp-per-sequence kernel (batched path)
     bool cluster = false;         // a thread-block cluster per group (latency of long sequences)
-    bool queue = false;           // dataflow schedule: one persistent launch, warps pulling (sequence, step, chunk)
+    bool queue = false;           // dataflow schedule (disabled: never set, see cf_queue.cu)
     int seats = 0;                // its sequences in progress per CTA
     int wgrid = 0;                // its grid
     int64_t slot_words = 0;       // its arena slot per warp
